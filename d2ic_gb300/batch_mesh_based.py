@@ -1,0 +1,117 @@
+"""Sequence runner (reference: d2ic/batch_base.py:9-52, d2ic/batch_mesh_based.py:25-282).
+
+``run(images) = end(sequence(images))`` after ``before(images)``; per frame:
+warm start (propagator, else the previous solution), optional chained local
+refinement pipeline, optional per-frame ``.npz`` (``u_nodal``, ``strain``).
+PNG export needs matplotlib, which this package does not use.
+"""
+from __future__ import annotations
+
+from abc import ABC, abstractmethod
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from .dataclasses import BatchConfig, BatchDiagnostics, BatchResult, DICResult
+from .dic_mesh_based import DICMeshBased
+from .mesh_assets import MeshAssets
+from .propagators import DisplacementPropagatorBase
+from .types import Array
+
+
+class BatchBase(ABC):
+    def run(self, images: Sequence[Array]) -> BatchResult:
+        self.before(images)
+        result = self.sequence(images)
+        return self.end(result)
+
+    @abstractmethod
+    def before(self, images: Sequence[Array]) -> None:
+        raise NotImplementedError
+
+    @abstractmethod
+    def sequence(self, images: Sequence[Array]) -> BatchResult:
+        raise NotImplementedError
+
+    @abstractmethod
+    def end(self, result: BatchResult) -> BatchResult:
+        raise NotImplementedError
+
+
+@dataclass
+class BatchState:
+    ref_image: Array
+    assets: MeshAssets
+    is_prepared: bool = False
+
+
+class BatchMeshBased(BatchBase):
+    def __init__(self, ref_image: Array, assets: MeshAssets, dic_mesh: DICMeshBased, batch_config: BatchConfig,
+                 dic_local: Optional[DICMeshBased] = None,
+                 propagator: Optional[DisplacementPropagatorBase] = None) -> None:
+        self.ref_image = ref_image
+        self.assets = assets
+        self.dic_mesh = dic_mesh
+        self.dic_local = dic_local
+        self.config = batch_config
+        self.propagator = propagator
+        self._state = BatchState(ref_image=ref_image, assets=assets, is_prepared=False)
+
+    def before(self, images) -> None:
+        self.dic_mesh.prepare(self.ref_image, self.assets)
+        if self.dic_local is not None:
+            self.dic_local.prepare(self.ref_image, self.assets)
+        self._state.is_prepared = True
+
+    def sequence(self, images: Sequence[Array] | Iterable[Array]) -> BatchResult:
+        if not self._state.is_prepared:
+            raise RuntimeError("BatchMeshBased.before() must be called before sequence().")
+        if bool(getattr(self.config, "export_png", False)):
+            raise ImportError("export_png needs matplotlib plotting, which is not part of this package")
+        save = bool(self.config.save_per_frame)
+        out_dir = None
+        if save:
+            out_dir = Path(self.config.per_frame_dir) if self.config.per_frame_dir else Path.cwd() / "_outputs" / "per_frame_fields"
+            out_dir.mkdir(parents=True, exist_ok=True)
+        verbose = bool(self.config.verbose)
+        progress = bool(self.config.progress)
+        try:
+            n_frames = len(images)  # type: ignore[arg-type]
+        except TypeError:
+            n_frames = None
+        per_frame: list[DICResult] = []
+        u_prev = None
+        u_prevprev = None
+        for k, Idef in enumerate(images):
+            if progress or verbose:
+                print(f"[Batch] Frame {k + 1}{'' if n_frames is None else '/' + str(n_frames)}: start")
+            if self.propagator is not None:
+                u_warm = self.propagator.propagate(u_prev=u_prev, u_prevprev=u_prevprev)
+            else:
+                u_warm = u_prev if self.config.warm_start_from_previous else None
+            if u_warm is not None:
+                self.dic_mesh.set_initial_guess(np.array(u_warm, copy=True))
+            res = self.dic_mesh.run(Idef)
+            if self.dic_local is not None:
+                self.dic_local.set_initial_guess(np.array(res.u_nodal, copy=True))
+                res = self.dic_local.run(Idef)
+            per_frame.append(res)
+            if save:
+                payload = {"u_nodal": np.asarray(res.u_nodal), "strain": np.asarray(res.strain)}
+                disc = (res.pixel_maps or {}).get("discrepancy_ref")
+                if disc is not None:
+                    payload["discrepancy_ref"] = np.asarray(disc)
+                np.savez_compressed(out_dir / f"frame_{k:04d}.npz", **payload)
+            u_prevprev = u_prev
+            u_prev = res.u_nodal
+            if progress or verbose:
+                print(f"[Batch] Frame {k + 1}{'' if n_frames is None else '/' + str(n_frames)}: done")
+        diag = BatchDiagnostics(info={"stage": "batch_mesh_based", "n_frames": len(per_frame),
+                                      "warm_start_from_previous": self.config.warm_start_from_previous})
+        return BatchResult(results=per_frame, diagnostics=diag)
+
+    def end(self, result: BatchResult) -> BatchResult:
+        return BatchResult(results=result.results,
+                           diagnostics=BatchDiagnostics(info={**result.diagnostics.info, "post": "end() placeholder"}))

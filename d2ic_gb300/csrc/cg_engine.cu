@@ -1,0 +1,751 @@
+// Persistent cooperative nonlinear-CG engine for the global FE-DIC objective.
+//
+// One launch solves a batch of independent frames (the plain GlobalCGSolver
+// drop-in is a batch of one).  All frames advance in lock-step "rounds"; one
+// round evaluates, for every active frame, the objective and its gradient at
+// the frame's current candidate point:
+//
+//   P phase  (pixels)  each warp takes chunks (<= 256 pixels of one element)
+//                      and computes, for the candidate u_c = u + alpha * dir,
+//                        r = I2(x + sum_a N_a u_c[a]) - I1,
+//                      the chunk's sum r^2 (FP64) and its 8 nodal gradient
+//                      partials sum r * dI2/dx * N_a (FP32).  No atomics on data.
+//   barrier
+//   N phase  (nodes)   per node: gather its chunk partials (node->chunk CSR),
+//                      add the spring gradient over the neighbour table,
+//                      write the trial gradient, trial point and trial
+//                      direction; per group of 512 nodes reduce (FP64, fixed
+//                      order) sum r^2, spring energy, g.g, g.(g - g_cur),
+//                      g_cur.dir.
+//   barrier + R        the last block to arrive reduces the group partials of
+//                      each frame (fixed order) and runs the CG control of
+//                      d2ic/solver_global_cg.py:362-461 (stop test, PR+ beta,
+//                      restart on g.d >= 0, Armijo with 10 halvings and the
+//                      forced 2^-10 step), then rebuilds the active list.
+//
+// Because every partial is written to its own slot and reduced in an order
+// fixed by the frame's own data layout, a frame's result does not depend on
+// which warps processed it or on which other frames shared the launch.
+//
+// The gradient at an accepted line-search point is produced by the same pass
+// that evaluated it, so an iteration costs one pixel pass per line-search
+// trial (the reference's separate value_and_grad pass is not repeated).
+//
+// Grid barriers are the engine's own (atomic counter + generation word) with a
+// globaltimer-bounded wait: a block that waits longer than D2IC_WAIT_NS sets
+// an abort flag and every block leaves the kernel at its next barrier.
+#include "common.cuh"
+
+namespace d2ic {
+
+constexpr int NG = D2IC_NODE_GROUP;            // threads per block == nodes per group
+constexpr int NWARP = NG / 32;
+constexpr unsigned long long WAIT_NS = 5ull * 1000ull * 1000ull * 1000ull;
+
+enum { ST_EVAL = 0, ST_TRIAL = 1, ST_FORCED = 2, ST_DONE = 3 };
+enum { P_JSUM = 0, P_EREG = 1, P_GG = 2, P_GDIFF = 3, P_GD = 4 };
+
+struct FrameState {
+    double J_cur, gg_cur, gg_prev, gdiff_cur, gd, J_last, gnorm;
+    float alpha, beta;
+    int state, k, t, restart, gd_known, nan_seen;
+    int iu, igp, igc, igt, idp;
+    int n_evals;
+};
+
+struct CtlHeader {
+    unsigned bar_count;
+    unsigned bar_gen;
+    int abort;
+    int err;
+    int n_active;
+    int total_chunks;
+    int total_groups;
+    int rounds;
+    unsigned work;
+    int max_rounds;
+    int pad_[6];
+};
+
+struct Ctl {
+    CtlHeader *h;
+    int *active;   // n_frames
+    int *cpre;     // n_frames + 1
+    int *gpre;     // n_frames + 1
+    FrameState *fs;
+};
+
+__host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+__host__ __device__ inline size_t ctl_layout(int n, size_t *o_active, size_t *o_cpre, size_t *o_gpre, size_t *o_fs) {
+    size_t off = align256(sizeof(CtlHeader));
+    *o_active = off;
+    off = align256(off + sizeof(int) * (size_t)n);
+    *o_cpre = off;
+    off = align256(off + sizeof(int) * (size_t)(n + 1));
+    *o_gpre = off;
+    off = align256(off + sizeof(int) * (size_t)(n + 1));
+    *o_fs = off;
+    off = align256(off + sizeof(FrameState) * (size_t)n);
+    return off;
+}
+
+__device__ inline Ctl make_ctl(char *base, int n) {
+    size_t oa, oc, og, of;
+    ctl_layout(n, &oa, &oc, &og, &of);
+    Ctl c;
+    c.h = (CtlHeader *)base;
+    c.active = (int *)(base + oa);
+    c.cpre = (int *)(base + oc);
+    c.gpre = (int *)(base + og);
+    c.fs = (FrameState *)(base + of);
+    return c;
+}
+
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ int ld_vol(const int *p) { return *(volatile const int *)p; }
+
+// Control data is rewritten by other blocks during the launch: read it through
+// L2 (never a possibly stale L1 line).
+__device__ __forceinline__ FrameState load_fs(const FrameState *p) {
+    static_assert(sizeof(FrameState) % 8 == 0, "FrameState size");
+    FrameState s;
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(p);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(&s);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(FrameState) / 8); ++i) dst[i] = __ldcg(src + i);
+    return s;
+}
+
+// node buffers of a frame: 0,1 = u ; 2,3,4 = g ; 5,6 = d
+__device__ __forceinline__ float2 *nbuf(const d2ic_frame_t &F, int j) {
+    return reinterpret_cast<float2 *>(F.node_ws) + (size_t)j * F.n_nodes;
+}
+
+// Candidate point of the current round: u (EVAL) or u + alpha * dir with
+// dir = -g (restart / first iteration) or -g + beta * d_prev.  Explicit
+// round-to-nearest operations so that the P and N phases produce identical bits.
+struct Cand {
+    const float2 *u, *g, *d;
+    float alpha, beta;
+    int mode;   // 0: u, 1: conjugate direction, 2: steepest descent
+    __device__ __forceinline__ float2 at(int n, float2 &dir) const {
+        const float2 un = __ldcg(u + n);
+        if (mode == 0) {
+            dir = make_float2(0.f, 0.f);
+            return un;
+        }
+        const float2 gn = __ldcg(g + n);
+        float dx = -gn.x, dy = -gn.y;
+        if (mode == 1) {
+            const float2 dn = __ldcg(d + n);
+            dx = __fadd_rn(dx, __fmul_rn(beta, dn.x));
+            dy = __fadd_rn(dy, __fmul_rn(beta, dn.y));
+        }
+        dir = make_float2(dx, dy);
+        return make_float2(__fadd_rn(un.x, __fmul_rn(alpha, dx)), __fadd_rn(un.y, __fmul_rn(alpha, dy)));
+    }
+};
+
+__device__ __forceinline__ Cand make_cand(const d2ic_frame_t &F, const FrameState *S) {
+    Cand c;
+    const int iu = ld_vol(&S->iu), igc = ld_vol(&S->igc), idp = ld_vol(&S->idp);
+    const int st = ld_vol(&S->state);
+    c.u = nbuf(F, iu);
+    c.g = nbuf(F, 2 + igc);
+    c.d = nbuf(F, 5 + idp);
+    c.alpha = *(volatile const float *)&S->alpha;
+    c.beta = *(volatile const float *)&S->beta;
+    const int k = ld_vol(&S->k), rs = ld_vol(&S->restart);
+    c.mode = (st == ST_EVAL) ? 0 : ((rs || k == 0) ? 2 : 1);
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// grid barrier (cooperative launch guarantees co-residency)
+// ---------------------------------------------------------------------------
+template <class F>
+__device__ bool grid_barrier(CtlHeader *H, F &&on_last) {
+    __shared__ int s_last;
+    __shared__ unsigned s_gen;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned gen = ld_acquire_u32(&H->bar_gen);
+        __threadfence();
+        const unsigned t = atomicAdd(&H->bar_count, 1u);
+        s_last = (t == gridDim.x - 1);
+        s_gen = gen;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        on_last();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            H->bar_count = 0;
+            __threadfence();
+            atomicExch(&H->bar_gen, s_gen + 1);
+        }
+    } else if (threadIdx.x == 0) {
+        const unsigned long long t0 = gtimer();
+        while (ld_acquire_u32(&H->bar_gen) == s_gen) {
+            if (ld_vol(&H->abort)) break;
+            if (gtimer() - t0 > WAIT_NS) {
+                H->err = D2IC_WAIT_TIMEOUT;
+                atomicExch(&H->abort, 1);
+                break;
+            }
+            __nanosleep(100);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ld_vol(&H->abort) == 0;
+}
+
+// largest s in [0, n) with pre[s] <= x (pre ascending, pre[0] == 0)
+__device__ __forceinline__ int find_slot(const int *pre, int n, int x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldcg(pre + mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// P phase: one chunk per warp
+// ---------------------------------------------------------------------------
+template <int KIND>
+__device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &cd, int c, int lane) {
+    const int pb = __ldg(F.chunk_begin + c), pe = __ldg(F.chunk_begin + c + 1);
+    float2 uc = make_float2(0.f, 0.f);
+    if (lane < 4) {
+        const int nd = __ldg(F.chunk_nodes + 4 * c + lane);
+        float2 dir;
+        uc = cd.at(nd, dir);
+    }
+    float ux[4], uy[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        ux[a] = __shfl_sync(0xffffffffu, uc.x, a);
+        uy[a] = __shfl_sync(0xffffffffu, uc.y, a);
+    }
+    const Img im{F.coeff, F.W, F.H, F.cpitch, F.pad};
+    const uint4 *pix = reinterpret_cast<const uint4 *>(F.pix);
+    float jr = 0.f;
+    float gxa[4] = {0.f, 0.f, 0.f, 0.f}, gya[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int p = pb + lane; p < pe; p += 32) {
+        const uint4 rec = __ldg(pix + p);
+        const int x = (int)(rec.x & 0xffffu), y = (int)(rec.x >> 16);
+        const float I1 = __uint_as_float(rec.y), xi = __uint_as_float(rec.z), eta = __uint_as_float(rec.w);
+        const float a0 = 0.5f * (1.f - xi), a1 = 0.5f * (1.f + xi);
+        const float b0 = 0.5f * (1.f - eta), b1 = 0.5f * (1.f + eta);
+        const float N[4] = {a0 * b0, a1 * b0, a1 * b1, a0 * b1};
+        const float dx = N[0] * ux[0] + N[1] * ux[1] + N[2] * ux[2] + N[3] * ux[3];
+        const float dy = N[0] * uy[0] + N[1] * uy[1] + N[2] * uy[2] + N[3] * uy[3];
+        int ix, iy;
+        float tx, ty;
+        split_coord(x, dx, ix, tx);
+        split_coord(y, dy, iy, ty);
+        float gx, gy;
+        const float v = sample<KIND>(im, ix, iy, tx, ty, gx, gy);
+        const float r = v - I1;
+        jr += r * r;
+        const float rgx = r * gx, rgy = r * gy;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            gxa[a] += rgx * N[a];
+            gya[a] += rgy * N[a];
+        }
+    }
+    const double js = warp_sum_d((double)jr);
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        gxa[a] = warp_sum_f(gxa[a]);
+        gya[a] = warp_sum_f(gya[a]);
+    }
+    if (lane == 0) {
+        F.chunk_J[c] = js;
+        float4 *cg = reinterpret_cast<float4 *>(F.chunk_grad + 8 * (size_t)c);
+        cg[0] = make_float4(gxa[0], gxa[1], gxa[2], gxa[3]);
+        cg[1] = make_float4(gya[0], gya[1], gya[2], gya[3]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// N phase: one group of NG nodes per block
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameState *S, int g, double (*red)[NWARP]) {
+    const Cand cd = make_cand(F, S);
+    const int n = g * NG + threadIdx.x;
+    const int igt = ld_vol(&S->igt), igc = ld_vol(&S->igc), iu = ld_vol(&S->iu), idp = ld_vol(&S->idp);
+    double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (n < F.n_nodes) {
+        float2 dir;
+        const float2 ui = cd.at(n, dir);
+        float sx = 0.f, sy = 0.f;
+        const int e0 = __ldg(F.node_chunk_ptr + n), e1 = __ldg(F.node_chunk_ptr + n + 1);
+        for (int e = e0; e < e1; ++e) {
+            const int ent = __ldg(F.node_chunk_ent + e);
+            const float *cgp = F.chunk_grad + 8 * (size_t)(ent >> 2) + (ent & 3);
+            sx += __ldcg(cgp);
+            sy += __ldcg(cgp + 4);
+        }
+        float rx = 0.f, ry = 0.f, en = 0.f;
+        const int md = F.max_deg;
+        for (int k = 0; k < md; ++k) {
+            const int j = __ldg(F.nbr_index + (size_t)n * md + k);
+            if (j < 0) break;
+            const float w = __ldg(F.nbr_weight + (size_t)n * md + k);
+            float2 dj;
+            const float2 uj = cd.at(j, dj);
+            const float ddx = ui.x - uj.x, ddy = ui.y - uj.y;
+            rx += w * ddx;
+            ry += w * ddy;
+            en += w * (ddx * ddx + ddy * ddy);
+        }
+        const float inv_np = 1.0f / (float)max(F.n_pix, 1);
+        const float gx = sx * inv_np + F.alpha_reg * rx;
+        const float gy = sy * inv_np + F.alpha_reg * ry;
+        nbuf(F, 2 + igt)[n] = make_float2(gx, gy);
+        nbuf(F, 1 - iu)[n] = ui;
+        nbuf(F, 5 + (1 - idp))[n] = dir;
+        const float2 gc = __ldcg(nbuf(F, 2 + igc) + n);
+        q[P_EREG] = 0.25 * (double)en;
+        q[P_GG] = (double)gx * gx + (double)gy * gy;
+        q[P_GDIFF] = (double)gx * ((double)gx - gc.x) + (double)gy * ((double)gy - gc.y);
+        q[P_GD] = (double)gc.x * dir.x + (double)gc.y * dir.y;
+    }
+    // this group's share of the chunk sums of r^2
+    {
+        const int c0 = g * F.chunks_per_group;
+        const int c1 = min(c0 + F.chunks_per_group, F.n_chunks);
+        for (int c = c0 + (int)threadIdx.x; c < c1; c += NG) q[P_JSUM] += __ldcg(F.chunk_J + c);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const double v = warp_sum_d(q[i]);
+        if (lane == 0) red[i][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double s = 0.0;
+        for (int w = 0; w < NWARP; ++w) s += red[threadIdx.x][w];
+        F.group_part[(size_t)g * D2IC_NPART + threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// R step (last block at the end-of-round barrier)
+// ---------------------------------------------------------------------------
+__device__ void hist_row(const d2ic_frame_t &F, int k, double a, double b, double c) {
+    if (F.hist && k < F.max_iter) {
+        F.hist[3 * k + 0] = (float)a;
+        F.hist[3 * k + 1] = (float)b;
+        F.hist[3 * k + 2] = (float)c;
+    }
+}
+
+__device__ void accept_point(FrameState &S, double J, double gg, double gdiff) {
+    S.J_cur = J;
+    S.gg_prev = S.gg_cur;
+    S.gg_cur = gg;
+    S.gdiff_cur = gdiff;
+    const int gp = S.igp;
+    S.igp = S.igc;
+    S.igc = S.igt;
+    S.igt = gp;
+    S.iu = 1 - S.iu;
+    S.idp = 1 - S.idp;
+}
+
+__device__ void start_iter(FrameState &S, const d2ic_frame_t &F) {
+    S.gnorm = sqrt(S.gg_cur);
+    if (S.gnorm < F.tol) {                       // stop branch: k unchanged
+        hist_row(F, S.k, S.J_cur, S.gnorm, 0.0);
+        S.state = ST_DONE;
+        return;
+    }
+    double beta = 0.0;
+    if (S.k > 0) {
+        const double x = S.gdiff_cur / (S.gg_prev + 1e-16);
+        beta = (x != x) ? x : fmax(x, 0.0);      // jnp.maximum keeps NaN
+    }
+    S.beta = (float)beta;
+    S.alpha = 1.0f;
+    S.t = 0;
+    S.restart = 0;
+    S.gd_known = 0;
+    S.state = ST_TRIAL;
+}
+
+__device__ void frame_decide(FrameState &S, const d2ic_frame_t &F, const double *q, int eval_only) {
+    const double J = 0.5 * q[P_JSUM] / (double)max(F.n_pix, 1) + (double)F.alpha_reg * q[P_EREG];
+    if (J != J || q[P_GG] != q[P_GG]) S.nan_seen = 1;
+    S.n_evals += 1;
+    switch (S.state) {
+        case ST_EVAL:
+            accept_point(S, J, q[P_GG], q[P_GDIFF]);
+            if (eval_only || F.max_iter <= 0) {
+                S.state = ST_DONE;
+                return;
+            }
+            start_iter(S, F);
+            return;
+        case ST_TRIAL: {
+            if (!S.gd_known) {
+                S.gd_known = 1;
+                S.gd = q[P_GD];
+                if (S.gd >= 0.0) {                 // not a descent direction: restart with -g
+                    S.restart = 1;
+                    S.gd = -S.gg_cur;
+                    S.alpha = 1.0f;
+                    return;                        // re-evaluate trial 0 along -g
+                }
+            }
+            if (J <= S.J_cur + 1e-4 * (double)S.alpha * S.gd) {
+                hist_row(F, S.k, J, S.gnorm, (double)S.alpha);
+                S.k += 1;
+                accept_point(S, J, q[P_GG], q[P_GDIFF]);
+                if (S.k >= F.max_iter) S.state = ST_DONE;
+                else start_iter(S, F);
+            } else {
+                S.J_last = J;
+                S.t += 1;
+                S.alpha *= 0.5f;
+                if (S.t >= 10) S.state = ST_FORCED;   // alpha == 2^-10 is applied anyway
+            }
+            return;
+        }
+        case ST_FORCED:
+            hist_row(F, S.k, S.J_last, S.gnorm, (double)S.alpha);
+            S.k += 1;
+            accept_point(S, J, q[P_GG], q[P_GDIFF]);
+            if (S.k >= F.max_iter) S.state = ST_DONE;
+            else start_iter(S, F);
+            return;
+        default:
+            return;
+    }
+}
+
+// rebuild the active list and prefix sums (whole block)
+__device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
+    __shared__ int s_cnt[NG], s_ch[NG], s_gr[NG];
+    const int per = (n_frames + NG - 1) / NG;
+    const int f0 = threadIdx.x * per, f1 = min(f0 + per, n_frames);
+    int cnt = 0, ch = 0, gr = 0;
+    for (int f = f0; f < f1; ++f)
+        if (ld_vol(&C.fs[f].state) != ST_DONE) {
+            ++cnt;
+            ch += frames[f].n_chunks;
+            gr += frames[f].n_groups;
+        }
+    s_cnt[threadIdx.x] = cnt;
+    s_ch[threadIdx.x] = ch;
+    s_gr[threadIdx.x] = gr;
+    __syncthreads();
+    if (threadIdx.x == 0) {   // exclusive scan (NG entries)
+        int a = 0, b = 0, c = 0;
+        for (int i = 0; i < NG; ++i) {
+            const int x = s_cnt[i], y = s_ch[i], z = s_gr[i];
+            s_cnt[i] = a; s_ch[i] = b; s_gr[i] = c;
+            a += x; b += y; c += z;
+        }
+        C.h->n_active = a;
+        C.h->total_chunks = b;
+        C.h->total_groups = c;
+        C.cpre[a] = b;
+        C.gpre[a] = c;
+    }
+    __syncthreads();
+    int slot = s_cnt[threadIdx.x], cp = s_ch[threadIdx.x], gp = s_gr[threadIdx.x];
+    for (int f = f0; f < f1; ++f)
+        if (ld_vol(&C.fs[f].state) != ST_DONE) {
+            C.active[slot] = f;
+            C.cpre[slot] = cp;
+            C.gpre[slot] = gp;
+            ++slot;
+            cp += frames[f].n_chunks;
+            gp += frames[f].n_groups;
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        C.h->work = 0;
+        C.h->rounds += 1;
+        if (C.h->rounds > C.h->max_rounds) {        // control-flow guard: never spin forever
+            C.h->err = D2IC_MAX_ITERS;
+            C.h->abort = 1;
+        }
+        __threadfence();
+    }
+}
+
+__device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
+    int mr = 0;
+    for (int f = threadIdx.x; f < n_frames; f += NG) {
+        FrameState S;
+        S.J_cur = S.gg_cur = S.gg_prev = S.gdiff_cur = S.gd = S.J_last = S.gnorm = 0.0;
+        S.alpha = 0.f;
+        S.beta = 0.f;
+        S.k = S.t = S.restart = S.gd_known = S.nan_seen = S.n_evals = 0;
+        S.iu = 0; S.igp = 0; S.igc = 1; S.igt = 2; S.idp = 0;
+        S.state = ST_EVAL;
+        C.fs[f] = S;
+        mr = max(mr, 12 * max(frames[f].max_iter, 0) + 4);
+    }
+    __shared__ int s_mr[NG];
+    s_mr[threadIdx.x] = mr;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int i = 0; i < NG; ++i) m = max(m, s_mr[i]);
+        C.h->max_rounds = m;
+        C.h->rounds = 0;
+    }
+    __syncthreads();
+    rebuild_active(frames, n_frames, C);
+}
+
+__device__ void r_step(const d2ic_frame_t *frames, int n_frames, Ctl &C, int eval_only) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int na = ld_vol(&C.h->n_active);
+    for (int s = wid; s < na; s += NWARP) {
+        const int f = ld_vol(C.active + s);
+        const d2ic_frame_t &F = frames[f];
+        double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int g = lane; g < F.n_groups; g += 32) {
+#pragma unroll
+            for (int i = 0; i < 5; ++i) q[i] += __ldcg(F.group_part + (size_t)g * D2IC_NPART + i);
+        }
+#pragma unroll
+        for (int i = 0; i < 5; ++i) q[i] = warp_sum_d(q[i]);
+        if (lane == 0) {
+            FrameState S = load_fs(C.fs + f);
+            frame_decide(S, F, q, eval_only);
+            C.fs[f] = S;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    rebuild_active(frames, n_frames, C);
+}
+
+// ---------------------------------------------------------------------------
+// the persistent kernel
+// ---------------------------------------------------------------------------
+template <int KIND>
+__global__ void __launch_bounds__(NG, 2) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
+                                                   char *ctl_base, int eval_only, const float *u_eval,
+                                                   double *J_out, float *grad_out) {
+    __shared__ double red[5][NWARP];
+    Ctl C = make_ctl(ctl_base, n_frames);
+    const int lane = threadIdx.x & 31;
+
+    // ---- init: u <- u0, zero g/d buffers, NaN history ----
+    for (int f = 0; f < n_frames; ++f) {
+        const d2ic_frame_t &F = frames[f];
+        const int nn = F.n_nodes;
+        const float2 *u0 = reinterpret_cast<const float2 *>((eval_only && u_eval && f == 0) ? u_eval : F.u0);
+        for (int i = blockIdx.x * NG + threadIdx.x; i < nn; i += gridDim.x * NG) {
+            nbuf(F, 0)[i] = u0 ? u0[i] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 1; j < 7; ++j) nbuf(F, j)[i] = make_float2(0.f, 0.f);
+        }
+        if (F.hist)
+            for (int i = blockIdx.x * NG + threadIdx.x; i < 3 * F.max_iter; i += gridDim.x * NG)
+                F.hist[i] = __int_as_float(0x7fc00000);
+    }
+    if (!grid_barrier(C.h, [&] { r_init(frames, n_frames, C); })) goto finish;
+
+    while (true) {
+        const int na = ld_vol(&C.h->n_active);
+        if (na == 0) break;
+        // ---- P phase ----
+        {
+            const int total = ld_vol(&C.h->total_chunks);
+            while (true) {
+                int c = 0;
+                if (lane == 0) c = (int)atomicAdd(&C.h->work, 1u);
+                c = __shfl_sync(0xffffffffu, c, 0);
+                if (c >= total) break;
+                const int s = find_slot(C.cpre, na, c);
+                const int f = __ldcg(C.active + s);
+                const d2ic_frame_t &F = frames[f];
+                const Cand cd = make_cand(F, C.fs + f);
+                pixel_chunk<KIND>(F, cd, c - __ldcg(C.cpre + s), lane);
+            }
+        }
+        if (!grid_barrier(C.h, [] {})) break;
+        // ---- N phase ----
+        {
+            const int tg = ld_vol(&C.h->total_groups);
+            for (int gi = blockIdx.x; gi < tg; gi += gridDim.x) {
+                const int s = find_slot(C.gpre, na, gi);
+                const int f = __ldcg(C.active + s);
+                node_group(frames[f], C.fs + f, gi - __ldcg(C.gpre + s), red);
+            }
+        }
+        if (!grid_barrier(C.h, [&] { r_step(frames, n_frames, C, eval_only); })) break;
+    }
+
+finish:
+    // ---- outputs ----
+    for (int f = 0; f < n_frames; ++f) {
+        const d2ic_frame_t &F = frames[f];
+        const FrameState *S = C.fs + f;
+        const int iu = ld_vol(&S->iu), igc = ld_vol(&S->igc);
+        const int nn = F.n_nodes;
+        float2 *uo = reinterpret_cast<float2 *>(F.u_out);
+        for (int i = blockIdx.x * NG + threadIdx.x; i < nn; i += gridDim.x * NG) {
+            if (uo) uo[i] = __ldcg(nbuf(F, iu) + i);
+            if (eval_only && grad_out && f == 0) reinterpret_cast<float2 *>(grad_out)[i] = __ldcg(nbuf(F, 2 + igc) + i);
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            if (F.n_iters) *F.n_iters = ld_vol(&S->k);
+            if (F.n_evals) *F.n_evals = ld_vol(&S->n_evals);
+            int st = D2IC_OK;
+            if (ld_vol(&C.h->abort)) st = ld_vol(&C.h->err);
+            else if (ld_vol(&S->nan_seen)) st = D2IC_NAN_DETECTED;
+            else if (ld_vol(&S->k) >= F.max_iter && F.max_iter > 0) st = D2IC_MAX_ITERS;
+            if (F.status) *F.status = st;
+            if (eval_only && J_out && f == 0) *J_out = *(volatile const double *)&S->J_cur;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <int KIND>
+static cudaError_t occupancy(int *blocks_per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cg_engine<KIND>, NG, 0);
+}
+
+struct DevInfo {
+    int sms = 0, bps[2] = {0, 0};
+};
+static DevInfo g_dev[64];
+
+static int dev_info(int dev, DevInfo **out) {
+    if (dev < 0 || dev >= 64) {
+        set_error("device index %d out of range", dev);
+        return D2IC_BAD_ARG;
+    }
+    DevInfo &d = g_dev[dev];
+    if (d.sms == 0) {
+        cudaError_t e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return cuda_status(e, "cudaDeviceGetAttribute");
+        e = occupancy<D2IC_INTERP_CUBIC>(&d.bps[0]);
+        if (e != cudaSuccess) return cuda_status(e, "occupancy");
+        e = occupancy<D2IC_INTERP_LINEAR>(&d.bps[1]);
+        if (e != cudaSuccess) return cuda_status(e, "occupancy");
+    }
+    *out = &d;
+    return D2IC_OK;
+}
+
+static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes, int kind,
+                         int grid_blocks, int eval_only, const float *u_eval, double *J_out, float *grad_out,
+                         cudaStream_t s) {
+    D2IC_REQUIRE(frames && control, "cg engine: null pointer");
+    D2IC_REQUIRE(n_frames >= 1 && n_frames <= D2IC_MAX_FRAMES, "cg engine: n_frames %d out of [1, %d]", n_frames,
+                 D2IC_MAX_FRAMES);
+    D2IC_REQUIRE(kind == D2IC_INTERP_CUBIC || kind == D2IC_INTERP_LINEAR, "cg engine: unknown interpolation %d", kind);
+    D2IC_REQUIRE(((uintptr_t)control & 255) == 0, "cg engine: control scratch must be 256-byte aligned");
+    const size_t need = d2ic_cg_control_bytes(n_frames);
+    D2IC_REQUIRE(control_bytes >= need, "cg engine: control scratch %zu bytes < %zu needed", control_bytes, need);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+    DevInfo *di = nullptr;
+    int st = dev_info(dev, &di);
+    if (st) return st;
+    const int maxb = di->sms * di->bps[kind == D2IC_INTERP_LINEAR];
+    D2IC_REQUIRE(maxb > 0, "cg engine: kernel cannot be resident on this device");
+    int blocks = grid_blocks > 0 ? (grid_blocks < maxb ? grid_blocks : maxb) : maxb;
+    e = cudaMemsetAsync(control, 0, sizeof(CtlHeader), s);
+    if (e != cudaSuccess) return cuda_status(e, "control reset");
+    char *cb = (char *)control;
+    void *args[] = {(void *)&frames, (void *)&n_frames, (void *)&cb, (void *)&eval_only, (void *)&u_eval,
+                    (void *)&J_out, (void *)&grad_out};
+    if (kind == D2IC_INTERP_CUBIC)
+        e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_CUBIC>, dim3(blocks), dim3(NG), args, 0, s);
+    else
+        e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_LINEAR>, dim3(blocks), dim3(NG), args, 0, s);
+    if (e != cudaSuccess) return cuda_status(e, "cudaLaunchCooperativeKernel(cg_engine)");
+    return D2IC_OK;
+}
+
+}  // namespace d2ic
+
+using namespace d2ic;
+
+extern "C" size_t d2ic_cg_control_bytes(int n_frames) {
+    if (n_frames < 1) n_frames = 1;
+    size_t a, b, c, d;
+    return ctl_layout(n_frames, &a, &b, &c, &d);
+}
+
+extern "C" size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks) {
+    const int ng = (n_nodes + NG - 1) / NG;
+    size_t off = align256(sizeof(float) * 14 * (size_t)n_nodes);
+    off += align256(sizeof(double) * (size_t)n_chunks);
+    off += align256(sizeof(float) * 8 * (size_t)n_chunks);
+    off += align256(sizeof(double) * D2IC_NPART * (size_t)(ng > 0 ? ng : 1));
+    return off;
+}
+
+extern "C" int d2ic_frame_bind_workspace(d2ic_frame_t *f, void *ws) {
+    D2IC_REQUIRE(f && ws, "d2ic_frame_bind_workspace: null pointer");
+    D2IC_REQUIRE(((uintptr_t)ws & 255) == 0, "d2ic_frame_bind_workspace: workspace must be 256-byte aligned");
+    D2IC_REQUIRE(f->n_nodes >= 1 && f->n_chunks >= 0, "d2ic_frame_bind_workspace: bad sizes");
+    char *p = (char *)ws;
+    f->node_ws = (float *)p;
+    p += align256(sizeof(float) * 14 * (size_t)f->n_nodes);
+    f->chunk_J = (double *)p;
+    p += align256(sizeof(double) * (size_t)f->n_chunks);
+    f->chunk_grad = (float *)p;
+    p += align256(sizeof(float) * 8 * (size_t)f->n_chunks);
+    f->group_part = (double *)p;
+    f->n_groups = (f->n_nodes + NG - 1) / NG;
+    f->chunks_per_group = (f->n_chunks + f->n_groups - 1) / f->n_groups;
+    return D2IC_OK;
+}
+
+extern "C" int d2ic_device_info(int device, int *num_sms, int *engine_blocks_per_sm) {
+    DevInfo *di = nullptr;
+    int st = dev_info(device, &di);
+    if (st) return st;
+    if (num_sms) *num_sms = di->sms;
+    if (engine_blocks_per_sm) *engine_blocks_per_sm = di->bps[0];
+    return D2IC_OK;
+}
+
+extern "C" int d2ic_cg_solve_batched(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
+                                     int interp_kind, int grid_blocks, void *stream) {
+    return launch_engine(frames, n_frames, control, control_bytes, interp_kind, grid_blocks, 0, nullptr, nullptr,
+                         nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int d2ic_eval_objective(const d2ic_frame_t *frame, const float *u, void *control, size_t control_bytes,
+                                   int interp_kind, double *J_out, float *grad_out, void *stream) {
+    D2IC_REQUIRE(u && J_out && grad_out, "d2ic_eval_objective: null pointer");
+    return launch_engine(frame, 1, control, control_bytes, interp_kind, 0, 1, u, J_out, grad_out,
+                         (cudaStream_t)stream);
+}

@@ -1,0 +1,141 @@
+// Shared device helpers of the d2ic_gb300 library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/d2ic_gb300.h"
+
+namespace d2ic {
+
+// ---- error reporting (thread-local message behind d2ic_last_error_string) ----
+void set_error(const char *fmt, ...);
+int cuda_status(cudaError_t e, const char *what);
+
+#define D2IC_CHECK_LAUNCH(what)                                       \
+    do {                                                              \
+        cudaError_t _e = cudaGetLastError();                          \
+        if (_e != cudaSuccess) return ::d2ic::cuda_status(_e, what);  \
+    } while (0)
+
+#define D2IC_REQUIRE(cond, ...)                 \
+    do {                                        \
+        if (!(cond)) {                          \
+            ::d2ic::set_error(__VA_ARGS__);     \
+            return D2IC_BAD_ARG;                \
+        }                                       \
+    } while (0)
+
+// ---- cubic B-spline weights for taps -1..2 at fractional offset t in [0,1) ----
+__device__ __forceinline__ void bspline_w(float t, float w[4], float dw[4]) {
+    const float t2 = t * t, t3 = t2 * t, o = 1.0f - t;
+    const float s = 1.0f / 6.0f;
+    w[0] = o * o * o * s;
+    w[1] = (3.0f * t3 - 6.0f * t2 + 4.0f) * s;
+    w[2] = (-3.0f * t3 + 3.0f * t2 + 3.0f * t + 1.0f) * s;
+    w[3] = t3 * s;
+    dw[0] = -0.5f * o * o;
+    dw[1] = 1.5f * t2 - 2.0f * t;
+    dw[2] = -1.5f * t2 + t + 0.5f;
+    dw[3] = 0.5f * t2;
+}
+
+struct Img {
+    const float *c;   // halo'd array
+    int W, H, cp, pad;
+    __device__ __forceinline__ float at(int r, int col) const {   // r, col: pixel indices (may be in the halo)
+        return __ldg(c + (size_t)(r + pad) * cp + (col + pad));
+    }
+};
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+
+// Cubic B-spline value and gradient at pixel (ix + tx, iy + ty), with integer
+// base (ix, iy) and fractional parts tx, ty in [0, 1).  Taps outside the halo'd
+// array clamp to its border, where the coefficients equal the edge value.
+__device__ __forceinline__ float sample_cubic(const Img &im, int ix, int iy, float tx, float ty,
+                                              float &gx, float &gy) {
+    float wx[4], dwx[4], wy[4], dwy[4];
+    bspline_w(tx, wx, dwx);
+    bspline_w(ty, wy, dwy);
+    float v = 0.f, ax = 0.f, ay = 0.f;
+    const int x0 = ix - 1, y0 = iy - 1;
+    if (x0 >= -im.pad && x0 + 3 < im.W + im.pad && y0 >= -im.pad && y0 + 3 < im.H + im.pad) {
+        const float *base = im.c + (size_t)(y0 + im.pad) * im.cp + (x0 + im.pad);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const float *row = base + (size_t)a * im.cp;
+            const float c0 = __ldg(row), c1 = __ldg(row + 1), c2 = __ldg(row + 2), c3 = __ldg(row + 3);
+            const float rv = wx[0] * c0 + wx[1] * c1 + wx[2] * c2 + wx[3] * c3;
+            const float rd = dwx[0] * c0 + dwx[1] * c1 + dwx[2] * c2 + dwx[3] * c3;
+            v += wy[a] * rv;
+            ax += wy[a] * rd;
+            ay += dwy[a] * rv;
+        }
+    } else {
+        int cx[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cx[b] = clampi(x0 + b, -im.pad, im.W - 1 + im.pad);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int r = clampi(y0 + a, -im.pad, im.H - 1 + im.pad);
+            const float c0 = im.at(r, cx[0]), c1 = im.at(r, cx[1]), c2 = im.at(r, cx[2]), c3 = im.at(r, cx[3]);
+            const float rv = wx[0] * c0 + wx[1] * c1 + wx[2] * c2 + wx[3] * c3;
+            const float rd = dwx[0] * c0 + dwx[1] * c1 + dwx[2] * c2 + dwx[3] * c3;
+            v += wy[a] * rv;
+            ax += wy[a] * rd;
+            ay += dwy[a] * rv;
+        }
+    }
+    gx = ax;
+    gy = ay;
+    return v;
+}
+
+// Bilinear value and gradient at pixel (ix + tx, iy + ty); taps clamped into the image.
+__device__ __forceinline__ float sample_linear(const Img &im, int ix, int iy, float tx, float ty,
+                                               float &gx, float &gy) {
+    const int x0 = clampi(ix, 0, im.W - 1), x1 = clampi(ix + 1, 0, im.W - 1);
+    const int y0 = clampi(iy, 0, im.H - 1), y1 = clampi(iy + 1, 0, im.H - 1);
+    const float i00 = im.at(y0, x0), i10 = im.at(y0, x1), i01 = im.at(y1, x0), i11 = im.at(y1, x1);
+    gx = (1.f - ty) * (i10 - i00) + ty * (i11 - i01);
+    gy = (1.f - tx) * (i01 - i00) + tx * (i11 - i10);
+    return (1.f - tx) * (1.f - ty) * i00 + tx * (1.f - ty) * i10 + (1.f - tx) * ty * i01 + tx * ty * i11;
+}
+
+template <int KIND>
+__device__ __forceinline__ float sample(const Img &im, int ix, int iy, float tx, float ty, float &gx, float &gy) {
+    if (KIND == D2IC_INTERP_LINEAR) return sample_linear(im, ix, iy, tx, ty, gx, gy);
+    return sample_cubic(im, ix, iy, tx, ty, gx, gy);
+}
+
+// floor(d) clamped to +-2^24 before the integer conversion, so that huge or
+// NaN coordinates give a far-outside (clamped) tap instead of a saturated
+// integer that could overflow the bounds arithmetic.  NaN propagates through
+// the fraction, never through an index.
+__device__ __forceinline__ float safe_floor(float d) {
+    return fminf(fmaxf(floorf(d), -16777216.0f), 16777216.0f);
+}
+
+// Split an image-index coordinate x = i + d (i integer pixel, d small
+// displacement) into integer base and fraction in [0,1) without forming the
+// rounded sum i + d.
+__device__ __forceinline__ void split_coord(int i, float d, int &ib, float &t) {
+    const float fl = safe_floor(d);
+    ib = i + (int)fl;
+    t = d - fl;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace d2ic

@@ -1,0 +1,276 @@
+"""GPU layout of a frame and launches of the CG engine.
+
+Data layout in HBM (per reference image + mesh, built once by
+:class:`FrameLayout`):
+
+* ``pix``   (Np, 16 B): element-major pixel records ``{col | row << 16, I1,
+  xi, eta}``, read with one 128-bit load; pixels of one element are
+  contiguous (in the reference's pixel order) and cut into chunks of at most
+  256 pixels;
+* ``chunk_begin`` (Nc+1), ``chunk_nodes`` (Nc, 4): chunk extents and the 4
+  nodes of the chunk's element;
+* ``node_chunk_ptr`` / ``node_chunk_ent``: node -> (chunk, local slot) CSR,
+  the transpose of the chunk -> node gather (no atomics);
+* ``nbr_index`` / ``nbr_weight``: the spring table, weights pre-multiplied by
+  (rho_i + rho_j)/2 in FP32.
+
+Per frame being solved (:class:`FrameSlot`): the deformed image's
+B-spline coefficients with a 16-pixel halo (row pitch a multiple of 32
+floats), the CG workspace, initial/final displacement, history and status.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ptr
+
+PAD = 16
+
+
+def _pitch(W: int) -> int:
+    return ((W + 2 * PAD + 31) // 32) * 32
+
+
+def interp_kind(interpolation: str) -> int:
+    v = str(interpolation).lower()
+    if v == "bilinear":
+        v = "linear"
+    if v == "cubic":
+        return _lib.INTERP_CUBIC
+    if v == "linear":
+        return _lib.INTERP_LINEAR
+    raise ValueError(f"Unsupported interpolation: {interpolation}")
+
+
+def as_device_image(img, device) -> torch.Tensor:
+    """float32 contiguous (H, W) image on ``device`` (host arrays are copied)."""
+    if isinstance(img, torch.Tensor):
+        t = img.to(device=device, dtype=torch.float32)
+    else:
+        a = np.asarray(img, dtype=np.float32)
+        t = torch.from_numpy(np.ascontiguousarray(a)).to(device, non_blocking=False)
+    if t.dim() != 2:
+        raise ValueError(f"expected a 2D image, got shape {tuple(t.shape)}")
+    return t.contiguous()
+
+
+def prepare_coefficients(img_dev: torch.Tensor, kind: int, out: torch.Tensor | None = None,
+                         tmp: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+    """Halo'd sampling array of an image: B-spline coefficients (cubic) or the padded image (linear)."""
+    H, W = img_dev.shape
+    cp = _pitch(W)
+    dev = img_dev.device
+    if out is None:
+        out = torch.empty((H + 2 * PAD, cp), dtype=torch.float32, device=dev)
+    s = _lib.stream_handle(stream)
+    if kind == _lib.INTERP_CUBIC:
+        if tmp is None:
+            tmp = torch.empty((H, cp), dtype=torch.float32, device=dev)
+        _lib.call("d2ic_bspline_prefilter", ptr(img_dev), H, W, PAD, cp, ptr(tmp), ptr(out), s)
+    else:
+        _lib.call("d2ic_pad_image", ptr(img_dev), H, W, PAD, cp, ptr(out), s)
+    return out
+
+
+def sample_points(coeff: torch.Tensor, H: int, W: int, kind: int, xy_index: torch.Tensor, stream=None):
+    """Value and gradient at image-index coordinates (x = col, y = row)."""
+    n = xy_index.shape[0]
+    dev = coeff.device
+    xy = xy_index.to(device=dev, dtype=torch.float32).contiguous()
+    v = torch.empty(n, dtype=torch.float32, device=dev)
+    gx = torch.empty_like(v)
+    gy = torch.empty_like(v)
+    _lib.call("d2ic_sample_points", ptr(coeff), H, W, PAD, coeff.shape[1], kind, ptr(xy), n, ptr(v), ptr(gx),
+              ptr(gy), _lib.stream_handle(stream))
+    return v, gx, gy
+
+
+def _xi_eta(pix) -> np.ndarray:
+    xe = getattr(pix, "xi_eta", None)
+    if xe is not None:
+        return np.asarray(xe, dtype=np.float64)
+    # Q4: N1 + N2 - N0 - N3 = xi and N2 + N3 - N0 - N1 = eta exactly
+    N = np.asarray(pix.pixel_shapeN, dtype=np.float64)
+    return np.stack([N[:, 1] + N[:, 2] - N[:, 0] - N[:, 3], N[:, 2] + N[:, 3] - N[:, 0] - N[:, 1]], axis=1)
+
+
+def _elements_of(pix) -> np.ndarray:
+    e = getattr(pix, "pixel_elts", None)
+    if e is not None:
+        return np.asarray(e, dtype=np.int64)
+    _, inv = np.unique(np.asarray(pix.pixel_nodes, dtype=np.int64), axis=0, return_inverse=True)
+    return inv.reshape(-1)
+
+
+class FrameLayout:
+    """Device-resident static data of one (reference image, mesh) pair."""
+
+    def __init__(self, pix, n_nodes: int, ref_image, interpolation: str = "cubic", device=None,
+                 chunk_max: int = _lib.CHUNK_MAX):
+        self.device = torch.device(device if device is not None else "cuda")
+        self.kind = interp_kind(interpolation)
+        self.n_nodes = int(n_nodes)
+        ref = as_device_image(ref_image, self.device)
+        self.H, self.W = ref.shape
+        if self.H >= 65536 or self.W >= 65536:
+            raise ValueError("image sides must be < 65536")
+        self.cpitch = _pitch(self.W)
+        pc = np.asarray(pix.pixel_coords_ref, dtype=np.float64)
+        pn = np.asarray(pix.pixel_nodes, dtype=np.int64)
+        Np = pc.shape[0]
+        self.n_pix = Np
+        elts = _elements_of(pix)
+        order = np.argsort(elts, kind="stable")                  # element-major, pixel order inside
+        e_sorted = elts[order]
+        # element runs -> chunks of <= chunk_max pixels (equal split of long runs)
+        if Np:
+            starts = np.flatnonzero(np.r_[True, e_sorted[1:] != e_sorted[:-1]])
+            lens = np.diff(np.r_[starts, Np])
+            nch = (lens + chunk_max - 1) // chunk_max
+            run = np.repeat(np.arange(starts.size), nch)
+            k = np.arange(nch.sum()) - np.repeat(np.cumsum(nch) - nch, nch)
+            cb = starts[run] + (lens[run] * k) // nch[run]
+            chunk_begin = np.r_[cb, Np].astype(np.int32)
+            chunk_nodes = pn[order[cb]].astype(np.int32)
+        else:
+            chunk_begin = np.zeros(1, np.int32)
+            chunk_nodes = np.zeros((0, 4), np.int32)
+        self.n_chunks = int(chunk_begin.size - 1)
+        # node -> (chunk, slot) CSR
+        flat = chunk_nodes.reshape(-1).astype(np.int64)
+        ent = (np.repeat(np.arange(self.n_chunks, dtype=np.int64), 4) << 2) | np.tile(np.arange(4), self.n_chunks)
+        o = np.argsort(flat, kind="stable")
+        cnt = np.bincount(flat, minlength=self.n_nodes)
+        self.node_chunk_ptr_h = np.r_[0, np.cumsum(cnt)].astype(np.int32)
+        node_chunk_ent = ent[o].astype(np.int32)
+        # spring table: entries beyond the degree are padding
+        nbi = np.asarray(pix.node_neighbor_index, dtype=np.int64).reshape(self.n_nodes, -1)
+        md = nbi.shape[1]
+        deg = np.asarray(pix.node_neighbor_degree, dtype=np.int64)
+        valid = np.arange(md)[None, :] < deg[:, None]
+        nid = np.where(valid, nbi, 0)
+        rho = np.asarray(pix.node_reg_weight, dtype=np.float32)
+        w = np.asarray(pix.node_neighbor_weight, dtype=np.float32).reshape(self.n_nodes, -1)
+        wc = (w * np.float32(0.5) * (rho[:, None] + rho[nid])).astype(np.float32)
+        self.max_deg = md
+        nbr_index = np.where(valid, nbi, -1).astype(np.int32)
+        nbr_weight = np.where(valid, wc, np.float32(0)).astype(np.float32)
+        # pixel records (I1 sampled on the device from the reference image)
+        colrow = np.stack([np.floor(pc[:, 0] - 0.5), np.floor(pc[:, 1] - 0.5)], axis=1).astype(np.int32)[order]
+        xieta = _xi_eta(pix).astype(np.float32)[order]
+        dev = self.device
+        T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        self.chunk_begin = T(chunk_begin)
+        self.chunk_nodes = T(chunk_nodes)
+        self.node_chunk_ptr = T(self.node_chunk_ptr_h)
+        self.node_chunk_ent = T(node_chunk_ent)
+        self.nbr_index = T(nbr_index)
+        self.nbr_weight = T(nbr_weight)
+        self.pixel_order = order
+        self.pix = torch.empty((max(Np, 1), 4), dtype=torch.int32, device=dev)
+        ref_coeff = prepare_coefficients(ref, self.kind)
+        if Np:
+            cr = T(colrow)
+            xe = T(xieta)
+            _lib.call("d2ic_pack_pixels", ptr(cr), ptr(xe), Np, ptr(ref_coeff), self.H, self.W, PAD, self.cpitch,
+                      self.kind, ptr(self.pix), _lib.stream_handle())
+        self.ref_image = ref
+        del ref_coeff
+
+    # bytes read per pixel per objective evaluation by the P phase (pixel record + ~1 coefficient)
+    PIX_BYTES = 16 + 4
+
+
+class FrameSlot:
+    """Per-solve device buffers and the frame descriptor."""
+
+    def __init__(self, layout: FrameLayout, max_iter: int):
+        self.layout = layout
+        dev = layout.device
+        L = layout
+        self.max_iter = int(max_iter)
+        self.coeff = torch.empty((L.H + 2 * PAD, L.cpitch), dtype=torch.float32, device=dev)
+        self.tmp = torch.empty((L.H, L.cpitch), dtype=torch.float32, device=dev) if L.kind == _lib.INTERP_CUBIC else None
+        self.u0 = torch.zeros((L.n_nodes, 2), dtype=torch.float32, device=dev)
+        self.u_out = torch.zeros((L.n_nodes, 2), dtype=torch.float32, device=dev)
+        self.hist = torch.full((max(self.max_iter, 1), 3), float("nan"), dtype=torch.float32, device=dev)
+        self.info = torch.zeros(3, dtype=torch.int32, device=dev)          # n_iters, status, n_evals
+        nb = _lib.load().d2ic_frame_workspace_bytes(L.n_nodes, L.n_chunks)
+        self.ws = torch.empty(nb, dtype=torch.uint8, device=dev)
+        self.desc = self._descriptor(1e-6, 0.0)
+
+    def _descriptor(self, tol: float, alpha_reg: float) -> _lib.Frame:
+        L = self.layout
+        f = _lib.Frame()
+        f.coeff = ptr(self.coeff)
+        f.pix = ptr(L.pix)
+        f.chunk_begin = ptr(L.chunk_begin)
+        f.chunk_nodes = ptr(L.chunk_nodes)
+        f.node_chunk_ptr = ptr(L.node_chunk_ptr)
+        f.node_chunk_ent = ptr(L.node_chunk_ent)
+        f.nbr_index = ptr(L.nbr_index)
+        f.nbr_weight = ptr(L.nbr_weight)
+        f.u0 = ptr(self.u0)
+        f.u_out = ptr(self.u_out)
+        f.hist = ptr(self.hist)
+        f.n_iters = ptr(self.info)
+        f.status = ptr(self.info) + 4
+        f.n_evals = ptr(self.info) + 8
+        f.tol = float(tol)
+        f.alpha_reg = float(alpha_reg)
+        f.max_iter = self.max_iter
+        f.W, f.H, f.cpitch, f.pad = L.W, L.H, L.cpitch, PAD
+        f.n_pix, f.n_chunks, f.n_nodes, f.max_deg = L.n_pix, L.n_chunks, L.n_nodes, L.max_deg
+        _lib.call("d2ic_frame_bind_workspace", ctypes.byref(f), ptr(self.ws))
+        return f
+
+    def set_params(self, tol: float, alpha_reg: float):
+        self.desc.tol = float(tol)
+        self.desc.alpha_reg = float(alpha_reg)
+
+    def load_image(self, def_image, stream=None):
+        img = as_device_image(def_image, self.layout.device)
+        prepare_coefficients(img, self.layout.kind, self.coeff, self.tmp, stream)
+
+    def set_u0(self, u0):
+        if u0 is None:
+            self.u0.zero_()
+        elif isinstance(u0, torch.Tensor):
+            self.u0.copy_(u0.reshape(-1, 2))
+        else:
+            self.u0.copy_(torch.from_numpy(np.ascontiguousarray(np.asarray(u0, dtype=np.float32).reshape(-1, 2))))
+
+
+def descriptors_to_device(descs, device) -> torch.Tensor:
+    """Pack frame descriptors into a device byte tensor (one d2ic_frame_t per frame)."""
+    n = len(descs)
+    arr = (_lib.Frame * n)(*descs)
+    buf = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8)
+    return buf.to(device)
+
+
+class Engine:
+    """Launch wrapper for batched solves: control scratch sized for up to ``max_frames``."""
+
+    def __init__(self, device, max_frames: int = 1):
+        self.device = torch.device(device)
+        self.max_frames = int(max_frames)
+        self.control = torch.empty(_lib.load().d2ic_cg_control_bytes(self.max_frames), dtype=torch.uint8,
+                                   device=self.device)
+
+    def solve(self, desc_dev: torch.Tensor, n_frames: int, kind: int, grid_blocks: int = 0, stream=None):
+        if n_frames > self.max_frames:
+            raise ValueError(f"{n_frames} frames > engine capacity {self.max_frames}")
+        _lib.call("d2ic_cg_solve_batched", ptr(desc_dev), n_frames, ptr(self.control), self.control.numel(), kind,
+                  grid_blocks, _lib.stream_handle(stream))
+
+    def eval_objective(self, desc_dev: torch.Tensor, u: torch.Tensor, kind: int, stream=None):
+        J = torch.zeros(1, dtype=torch.float64, device=self.device)
+        g = torch.empty_like(u)
+        _lib.call("d2ic_eval_objective", ptr(desc_dev), ptr(u), ptr(self.control), self.control.numel(), kind,
+                  ptr(J), ptr(g), _lib.stream_handle(stream))
+        return J, g

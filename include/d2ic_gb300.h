@@ -1,0 +1,166 @@
+/*
+ * d2ic_gb300 — C ABI of the GB300 (sm_103a) global finite-element DIC hot path.
+ *
+ * Plain C: pointers, sizes and a CUDA stream handle passed as `void *`
+ * (a cudaStream_t; NULL = legacy default stream).  Every device pointer is
+ * borrowed for the duration of the call; the library never frees caller
+ * memory.  Functions return D2IC_OK (0) or a negative status; the message of
+ * the last failure on the calling thread is d2ic_last_error_string().
+ * Nothing here throws across the ABI.
+ *
+ * The entry points replace the reference's JAX kernels behind the solver
+ * plugin interface `SolverBase.compile/solve` (d2ic/solver_base.py:8-26).
+ * Each declaration names the reference code it replaces.
+ */
+#ifndef D2IC_GB300_H
+#define D2IC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define D2IC_API __attribute__((visibility("default")))
+#else
+#define D2IC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define D2IC_OK             0
+#define D2IC_BAD_ARG       -1   /* maps to ValueError on the Python side      */
+#define D2IC_OOM           -2
+#define D2IC_NAN_DETECTED  -3   /* reported in per-frame status, not raised   */
+#define D2IC_MAX_ITERS     -4   /* reported in per-frame status, not raised   */
+#define D2IC_WAIT_TIMEOUT  -5   /* a bounded device-side wait gave up         */
+#define D2IC_CUDA_ERROR    -6
+#define D2IC_UNSUPPORTED   -7
+
+/* interpolation kinds (GlobalCGSolver(interpolation=...)) */
+#define D2IC_INTERP_CUBIC   0   /* cubic B-spline, edge-replicating boundary  */
+#define D2IC_INTERP_LINEAR  1   /* bilinear, edge clamped                     */
+
+/* sizes of the engine's fixed-shape pieces */
+#define D2IC_NODE_GROUP   512   /* nodes per reduction group (= block size)   */
+#define D2IC_NPART          6   /* doubles per group partial                  */
+#define D2IC_MAX_FRAMES  4096   /* frames per batched launch                  */
+#define D2IC_CHUNK_MAX    256   /* pixels per chunk (one element per chunk)   */
+
+/* One pixel of the element-major pixel list: 16 bytes, read with one 128-bit load. */
+typedef struct d2ic_pixrec {
+    uint32_t pos;     /* column | (row << 16) of the pixel                     */
+    float    I1;      /* reference-image sample at the pixel centre            */
+    float    xi;      /* local element coordinates of the pixel centre         */
+    float    eta;
+} d2ic_pixrec_t;
+
+/*
+ * Everything one frame's solve reads and writes.  All pointers are device
+ * pointers.  The workspace fields are set by d2ic_frame_bind_workspace().
+ */
+typedef struct d2ic_frame {
+    /* deformed image: B-spline coefficients (cubic) or the image itself (linear),
+     * with a `pad`-wide halo; pixel (i,j) lives at coeff[(i+pad)*cpitch + j+pad] */
+    const float *coeff;
+    /* element-major pixel list, cut into chunks of <= D2IC_CHUNK_MAX pixels of one element */
+    const d2ic_pixrec_t *pix;
+    const int   *chunk_begin;      /* n_chunks + 1                                      */
+    const int   *chunk_nodes;      /* 4 * n_chunks, the chunk's element nodes (Q4 order) */
+    const int   *node_chunk_ptr;   /* n_nodes + 1                                       */
+    const int   *node_chunk_ent;   /* (chunk << 2) | local node slot, by node           */
+    const int   *nbr_index;        /* n_nodes * max_deg spring neighbours, -1 padded    */
+    const float *nbr_weight;       /* w_ij * (rho_i + rho_j) / 2                        */
+    const float *u0;               /* 2 * n_nodes initial displacement                  */
+    float       *u_out;            /* 2 * n_nodes solution                              */
+    float       *hist;             /* 3 * max_iter CG history [J, |g|, alpha], NaN-filled */
+    int         *n_iters;          /* 1: iterations taken                               */
+    int         *status;           /* 1: D2IC_OK / D2IC_NAN_DETECTED / D2IC_MAX_ITERS   */
+    int         *n_evals;          /* 1: objective evaluations (pixel passes) performed */
+    /* workspace */
+    float       *node_ws;          /* 14 * n_nodes floats                               */
+    double      *chunk_J;          /* n_chunks                                          */
+    float       *chunk_grad;       /* 8 * n_chunks                                      */
+    double      *group_part;       /* D2IC_NPART * n_groups                             */
+    double       tol;
+    float        alpha_reg;
+    int          max_iter;
+    int          W, H, cpitch, pad;
+    int          n_pix, n_chunks, n_nodes, max_deg;
+    int          n_groups, chunks_per_group;
+} d2ic_frame_t;
+
+/* ---- library ------------------------------------------------------------- */
+D2IC_API const char *d2ic_last_error_string(void);
+D2IC_API int d2ic_version(void);
+/* SM count and the persistent engine's resident blocks per SM on `device`. */
+D2IC_API int d2ic_device_info(int device, int *num_sms, int *engine_blocks_per_sm);
+
+/* ---- image preparation (replaces the per-call sampling setup inside
+ *      im_jax.flat_nd_cubic_interpolate, d2ic/solver_global_cg.py:512-518) ---- */
+
+/* Cubic B-spline coefficients of an HxW float image extended by edge
+ * replication, written with a `pad`-wide halo into coeff ((H+2pad) x cpitch).
+ * tmp: H x cpitch floats of scratch.  pad >= 16, cpitch >= W + 2 pad. */
+D2IC_API int d2ic_bspline_prefilter(const float *img, int H, int W, int pad, int cpitch,
+                           float *tmp, float *coeff, void *stream);
+
+/* Copy an image into the halo layout with edge replication (linear kind). */
+D2IC_API int d2ic_pad_image(const float *img, int H, int W, int pad, int cpitch, float *out, void *stream);
+
+/* Sample n points at image-index coordinates xy (x = col, y = row, i.e. the
+ * reference's pixel-centre coordinates minus 0.5); value and d/dx, d/dy.
+ * Replaces _cubic_sample / _bilinear_sample (d2ic/solver_global_cg.py:481-518). */
+D2IC_API int d2ic_sample_points(const float *coeff, int H, int W, int pad, int cpitch, int kind,
+                       const float *xy, int n, float *val, float *gx, float *gy, void *stream);
+
+/* Build the 16-byte pixel records: pos from (col,row) pairs, I1 sampled from
+ * the reference-image coefficients at the pixel centre, (xi,eta) copied. */
+D2IC_API int d2ic_pack_pixels(const int *colrow, const float *xieta, int n,
+                     const float *coeff1, int H, int W, int pad, int cpitch, int kind,
+                     d2ic_pixrec_t *out, void *stream);
+
+/* ---- global CG engine (replaces _cg_solve / _J_TOTAL_VG / J_total,
+ *      d2ic/solver_global_cg.py:289-469, behind GlobalCGSolver.solve :151-198) ---- */
+
+/* Bytes of per-frame workspace, and binding of a workspace block to a frame
+ * descriptor (host-side; `ws` is a device pointer aligned to 256 bytes). */
+D2IC_API size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks);
+D2IC_API int d2ic_frame_bind_workspace(d2ic_frame_t *frame, void *ws);
+
+/* Bytes of launch-wide control scratch for a batched launch of n_frames. */
+D2IC_API size_t d2ic_cg_control_bytes(int n_frames);
+
+/* Solve n_frames independent frames in ONE persistent cooperative launch.
+ * frames: device array of n_frames descriptors.  control: device scratch of
+ * d2ic_cg_control_bytes(n_frames) bytes (the call clears it on `stream`).
+ * grid_blocks: 0 = all resident blocks.  Per-frame results land in each
+ * descriptor's u_out / hist / n_iters / status. */
+D2IC_API int d2ic_cg_solve_batched(const d2ic_frame_t *frames, int n_frames, void *control,
+                          size_t control_bytes, int interp_kind, int grid_blocks, void *stream);
+
+/* Objective and gradient at u for one frame (the value_and_grad of J_total,
+ * d2ic/solver_global_cg.py:323).  frame: device pointer; control: as above for
+ * one frame.  Writes J (1 double) and grad (2*n_nodes floats). */
+D2IC_API int d2ic_eval_objective(const d2ic_frame_t *frame, const float *u, void *control, size_t control_bytes,
+                        int interp_kind, double *J_out, float *grad_out, void *stream);
+
+/* ---- initial motion (replaces _match_centers_jax, d2ic/solver_translation_zncc.py:118-168,
+ *      and _project_centers_to_nodes_idw, d2ic/dic_init_motion.py:64-91) ---- */
+D2IC_API int d2ic_zncc_match(const float *ref, int Hr, int Wr, const float *def, int Hd, int Wd,
+                    const float *centers, int n_centers, int win, int search,
+                    float *u_out, float *score_out, void *stream);
+D2IC_API int d2ic_idw_project(const float *nodes, int n_nodes, const float *centers, const float *disp,
+                     int n_centers, float power, float *u_out, void *stream);
+
+/* ---- strain (replaces compute_green_lagrange_strain_nodes_lsq + green_lagrange_to_voigt,
+ *      d2ic/strain.py:11-114) ---- */
+D2IC_API int d2ic_strain_gl(const float *u, const float *nodes, const int *nbr_index, const int *nbr_degree,
+                   int n_nodes, int max_deg, float gauge_length, float eps,
+                   float *voigt_out, float *F_out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* D2IC_GB300_H */

@@ -1,0 +1,32 @@
+"""The C-ABI library loads and exports every symbol declared in include/d2ic_gb300.h (no GPU needed)."""
+from __future__ import annotations
+
+import ctypes
+
+
+def test_library_exports_header_symbols(built_library):
+    from d2ic_gb300 import _lib
+    names = _lib.header_symbols()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(built_library, n)]
+    assert not missing, f"symbols declared but not exported: {missing}"
+    # every declared symbol has a ctypes signature on the Python side
+    assert set(names) <= set(_lib._SIGS)
+
+
+def test_host_only_entry_points(built_library):
+    """Size queries and workspace binding run on the host."""
+    from d2ic_gb300 import _lib
+    assert built_library.d2ic_version() >= 100
+    assert built_library.d2ic_cg_control_bytes(1) > 0
+    assert built_library.d2ic_cg_control_bytes(64) > built_library.d2ic_cg_control_bytes(1)
+    nb = built_library.d2ic_frame_workspace_bytes(1089, 784)
+    assert nb >= 14 * 4 * 1089 + 784 * (8 + 32)
+    f = _lib.Frame()
+    f.n_nodes, f.n_chunks = 1089, 784
+    fake_ws = 1 << 20                      # never dereferenced: binding only computes addresses
+    assert built_library.d2ic_frame_bind_workspace(ctypes.byref(f), fake_ws) == 0
+    assert f.node_ws == fake_ws and f.n_groups == 3 and f.chunks_per_group == 262
+    assert f.chunk_J % 256 == 0 and f.chunk_grad % 256 == 0 and f.group_part % 256 == 0
+    assert built_library.d2ic_frame_bind_workspace(ctypes.byref(f), fake_ws + 8) == _lib.BAD_ARG
+    assert b"256-byte" in built_library.d2ic_last_error_string()
