@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark of the global FE-DIC hot path on GB300.
+
+Workload (default ``plate_hole_2048``): 2048^2 synthetic speckle, 1800^2
+square minus an r = 300 disk, 16 px Q4 elements (16,641 nodes, 2.92 M ROI
+pixels), 20 frames of the plate-hole field; frame 0 initialised by ZNCC +
+IDW, later frames warm-started from the previous solution; CG tol 1e-3,
+reg 0.1, max 200 iterations.  One step = the whole 20-frame sequence.
+
+* ``value``: frames/s with the images already in HBM (device-resident
+  sequence path), L2 flushed (256 MB write) between steps;
+* ``e2e``: the same frames/s through the public API (DICInitMotion for frame
+  0, then BatchMeshBased.run) from pinned host frames, per-frame device->host
+  results included; per-frame p50/p99 latency reported beside it;
+* ``roofline``: the persistent CG kernel's algorithmic bytes (48 B per ROI
+  pixel and 128 B per node per objective evaluation) over its CUDA-event
+  duration, against the measured HBM copy bandwidth;
+* ``cpu_baseline``: the FP64 oracle restatement (C, OpenMP) on the host cores
+  over a bounded sample of the same sequence.
+
+``--impl reference`` times that CPU restatement alone (the reference itself is
+JAX and cannot be installed offline).  Multi-GPU: one independent replica
+sequence per rank (frames shard by sequence, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+B_PIX = 48      # algorithmic bytes per ROI pixel per objective evaluation
+B_NODE = 128    # spring matvec (80) + CG vector ops (48) per node per evaluation
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", default="plate_hole_2048",
+                   choices=["plate_hole_2048", "plate_hole_4096", "translation_512"])
+    p.add_argument("--frames", type=int, default=20)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-sample-frames", type=int, default=2)
+    return p.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
+def make_workload(name: str, n_frames: int, seed: int, device):
+    from d2ic_gb300 import workloads
+    if name == "plate_hole_2048":
+        return workloads.plate_hole_2048(n_frames=n_frames, seed=seed, device=device)
+    if name == "plate_hole_4096":     # same field scaled to 4096^2: pixel data larger than L2 (profiling case)
+        return workloads.plate_hole_2048(n_frames=n_frames, seed=seed, device=device, H=4096)
+    return workloads.translation_512(seed=seed, device=device)
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement (oracle) leg
+# ---------------------------------------------------------------------------
+
+def cpu_sequence_sample(wl, n_sample: int, u_start=None):
+    """Time the FP64 oracle (C pixel term, OpenMP on all host cores) on frames 1..n_sample."""
+    from oracle import fast, objective, pixels
+    H, W = wl.ref.shape
+    oa = pixels.build_pixel_assets(np.asarray(wl.mesh.nodes_xy), np.asarray(wl.mesh.elements), H, W,
+                                   wl.assets.roi_mask)
+    cfg = wl.config
+    frames = list(range(1, min(n_sample, len(wl.frames) - 1) + 1)) if len(wl.frames) > 1 else [0]
+    u = np.zeros((wl.n_nodes, 2)) if u_start is None else np.asarray(u_start, np.float64)
+    t_solve = 0.0
+    iters = []
+    for k in frames:
+        pb = objective.Problem.build(wl.ref, wl.frames[k], oa)        # coefficients: setup, not timed
+        fp = fast.FastProblem(pb)
+        t0 = time.perf_counter()
+        u, h, kk, ne = fp.cg_solve(u, cfg.reg_strength, cfg.max_iters, cfg.tol)
+        t_solve += time.perf_counter() - t0
+        iters.append(int(kk))
+    cores = os.cpu_count() or 1
+    return {"value": len(frames) / t_solve, "unit": "frames/s", "cores": cores, "kind": "port",
+            "sample": f"{wl.name}: frames {frames[0]}..{frames[-1]} warm-started, FP64 C oracle CG "
+                      f"({cores} OpenMP threads), {sum(iters)} iterations in {t_solve:.1f} s"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    wl = make_workload(args.workload, min(args.frames, 1 + args.cpu_sample_frames), 1, dev)
+    # each sample is 10-30 s of CPU work: at most two of them, however many steps were asked for
+    vals = []
+    for _ in range(max(1, min(args.steps, 2))):
+        r = cpu_sequence_sample(wl, args.cpu_sample_frames)
+        vals.append(r["value"])
+    v = statistics.median(vals)
+    line = {"metric": "frames/s", "value": v, "unit": "frames/s", "n_gpus": args.gpus, "steps": len(vals),
+            "warmup": 0, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": wl.name, "frames": args.frames},
+            "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference is JAX; jax/im_jax cannot be installed offline, so this arm times the "
+                    "project's FP64 C restatement of its CG solve on the host cores"}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+
+def run_ours(args, ws, rank, local):
+    import torch
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300.sequence import SequenceRunner
+
+    dev = torch.device("cuda", local)
+    wl = make_workload(args.workload, args.frames, 1 + rank, dev)
+    solver = d2.GlobalCGSolver(device=dev)
+    dic = d2.DICMeshBased(wl.mesh, solver, wl.config)
+    dic.prepare(wl.ref, wl.assets)
+    runner = SequenceRunner(solver, dic.state)
+    frames_dev = [torch.from_numpy(f).to(dev) for f in wl.frames]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    nF = len(frames_dev)
+
+    def step(time_engine=False):
+        return runner.run(frames_dev, init_cfg=wl.init, propagation="previous", time_engine=time_engine)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    engine_ms = []
+    evals = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        res = step(time_engine=True)
+        e1.record()
+        barrier(ws)
+        times.append(e0.elapsed_time(e1) / 1000.0)
+        engine_ms.extend(a.elapsed_time(b) for a, b in res.engine_events)
+        evals.extend(res.info[:, 2].cpu().tolist())
+    clk = clocks.stop()
+    t_step = max_over_ranks(statistics.median(times), ws)
+    value = ws * nF / t_step
+    iters = res.info[:, 0].cpu().tolist()
+
+    # roofline of the persistent CG kernel
+    peak, peak_src = peaks()
+    bytes_per_eval = B_PIX * wl.n_pix + B_NODE * wl.n_nodes
+    achieved = (sum(evals) * bytes_per_eval / 1e9) / (sum(engine_ms) / 1000.0)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "peak_source": peak_src, "kernel": "cg_engine<cubic>",
+            "launch_ms_mean": statistics.mean(engine_ms), "evals_per_launch": statistics.mean(evals),
+            "bytes_per_eval": bytes_per_eval}
+    prof = os.path.join(ROOT, "profiles", "cg_engine_plate_hole_2048.txt")
+    if os.path.exists(prof):
+        for ln in open(prof):
+            if ln.startswith("dram_bytes_per_eval:"):
+                roof["traffic"] = float(ln.split(":")[1]) * statistics.mean(evals)
+
+    out = {"metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_step * 1000.0, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 (f64 CG reductions)", "data": "synthetic",
+           "config": {"workload": wl.name, "frames": nF, "image": list(wl.ref.shape), "roi_pixels": wl.n_pix,
+                      "nodes": wl.n_nodes, "element_px": 16, "tol": wl.config.tol, "reg": wl.config.reg_strength,
+                      "max_iters": wl.config.max_iters, "l2": "flushed (256 MB write) between steps",
+                      "parallelism": f"replicas x{ws}"},
+           "cg_iterations_per_frame": statistics.mean(iters),
+           "gpu_launches": nF * 4 + 2, "roofline": roof}
+    if clk:
+        out["clocks"] = clk
+
+    # e2e through the public API with pinned host frames
+    if not args.no_e2e:
+        pinned = [torch.from_numpy(f).pin_memory() for f in wl.frames]
+        init = d2.DICInitMotion(wl.init, d2.TranslationZNCCSolver(wl.init, device=dev))
+        init.prepare(wl.ref, dic.state.assets)
+        batch = d2.BatchMeshBased(wl.ref, dic.state.assets, dic, d2.BatchConfig(warm_start_from_previous=True))
+        batch.before(pinned)
+
+        def e2e_step():
+            r0 = init.run(pinned[0])
+            dic.set_initial_guess(r0.u_nodal)
+            lat = []
+            res = batch.sequence(pinned, latencies=lat)
+            return res, lat
+
+        for _ in range(max(1, args.warmup - 1)):
+            e2e_step()
+        et = []
+        lats = []
+        for _ in range(args.steps):
+            barrier(ws)
+            t0 = time.perf_counter()
+            res_b, lat = e2e_step()
+            barrier(ws)
+            et.append(time.perf_counter() - t0)
+            lats.extend(lat)
+        te = max_over_ranks(statistics.median(et), ws)
+        Nn = wl.n_nodes
+        out["e2e"] = {"value": ws * nF / te, "unit": "frames/s",
+                      "h2d_bytes_per_step": int(sum(f.nbytes for f in wl.frames)),
+                      "d2h_bytes_per_step": int(nF * (Nn * 2 * 4 + Nn * 3 * 4 + wl.config.max_iters * 12 + 12)
+                                                + Nn * 2 * 4),
+                      "latency_ms_p50": 1000 * float(np.percentile(lats, 50)),
+                      "latency_ms_p99": 1000 * float(np.percentile(lats, 99))}
+        u_dev = res.u.cpu().numpy()
+        u_api = np.stack([np.asarray(r.u_nodal) for r in res_b.results])
+        out["e2e"]["max_abs_diff_vs_value_path_px"] = float(np.abs(u_dev - u_api).max())
+
+    if not args.no_cpu and rank == 0:
+        cb = cpu_sequence_sample(wl, args.cpu_sample_frames, u_start=res.u[0].cpu().numpy())
+        out["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -65,7 +65,9 @@ class BatchMeshBased(BatchBase):
             self.dic_local.prepare(self.ref_image, self.assets)
         self._state.is_prepared = True
 
-    def sequence(self, images: Sequence[Array] | Iterable[Array]) -> BatchResult:
+    def sequence(self, images: Sequence[Array] | Iterable[Array], latencies: list | None = None) -> BatchResult:
+        """Per-frame loop; ``latencies`` (optional list) receives each frame's wall time in seconds."""
+        import time
         if not self._state.is_prepared:
             raise RuntimeError("BatchMeshBased.before() must be called before sequence().")
         if bool(getattr(self.config, "export_png", False)):
@@ -85,6 +87,7 @@ class BatchMeshBased(BatchBase):
         u_prev = None
         u_prevprev = None
         for k, Idef in enumerate(images):
+            t0 = time.perf_counter()
             if progress or verbose:
                 print(f"[Batch] Frame {k + 1}{'' if n_frames is None else '/' + str(n_frames)}: start")
             if self.propagator is not None:
@@ -98,6 +101,8 @@ class BatchMeshBased(BatchBase):
                 self.dic_local.set_initial_guess(np.array(res.u_nodal, copy=True))
                 res = self.dic_local.run(Idef)
             per_frame.append(res)
+            if latencies is not None:
+                latencies.append(time.perf_counter() - t0)
             if save:
                 payload = {"u_nodal": np.asarray(res.u_nodal), "strain": np.asarray(res.strain)}
                 disc = (res.pixel_maps or {}).get("discrepancy_ref")
