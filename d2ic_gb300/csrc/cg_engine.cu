@@ -444,9 +444,33 @@ __device__ void frame_decide(FrameState &S, const d2ic_frame_t &F, const double 
     }
 }
 
+// exclusive block-wide scan of three counters (warp shuffles + one shared pass)
+__device__ __forceinline__ void block_scan3(int &a, int &b, int &c, int &ta, int &tb, int &tc) {
+    __shared__ int s_w[NWARP][3];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int ia = a, ib = b, ic = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o),
+                  xc = __shfl_up_sync(0xffffffffu, ic, o);
+        if (lane >= o) { ia += xa; ib += xb; ic += xc; }
+    }
+    if (lane == 31) { s_w[wid][0] = ia; s_w[wid][1] = ib; s_w[wid][2] = ic; }
+    __syncthreads();
+    int oa = 0, ob = 0, oc = 0;
+    ta = tb = tc = 0;
+    for (int w = 0; w < NWARP; ++w) {
+        if (w == wid) { oa = ta; ob = tb; oc = tc; }
+        ta += s_w[w][0]; tb += s_w[w][1]; tc += s_w[w][2];
+    }
+    a = oa + ia - a;
+    b = ob + ib - b;
+    c = oc + ic - c;
+    __syncthreads();
+}
+
 // rebuild the active list and prefix sums (whole block)
 __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
-    __shared__ int s_cnt[NG], s_ch[NG], s_gr[NG];
     const int per = (n_frames + NG - 1) / NG;
     const int f0 = threadIdx.x * per, f1 = min(f0 + per, n_frames);
     int cnt = 0, ch = 0, gr = 0;
@@ -456,25 +480,16 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
             ch += frames[f].n_chunks;
             gr += frames[f].n_groups;
         }
-    s_cnt[threadIdx.x] = cnt;
-    s_ch[threadIdx.x] = ch;
-    s_gr[threadIdx.x] = gr;
-    __syncthreads();
-    if (threadIdx.x == 0) {   // exclusive scan (NG entries)
-        int a = 0, b = 0, c = 0;
-        for (int i = 0; i < NG; ++i) {
-            const int x = s_cnt[i], y = s_ch[i], z = s_gr[i];
-            s_cnt[i] = a; s_ch[i] = b; s_gr[i] = c;
-            a += x; b += y; c += z;
-        }
-        C.h->n_active = a;
-        C.h->total_chunks = b;
-        C.h->total_groups = c;
-        C.cpre[a] = b;
-        C.gpre[a] = c;
+    int ta, tb, tc;
+    block_scan3(cnt, ch, gr, ta, tb, tc);
+    if (threadIdx.x == 0) {
+        C.h->n_active = ta;
+        C.h->total_chunks = tb;
+        C.h->total_groups = tc;
+        C.cpre[ta] = tb;
+        C.gpre[ta] = tc;
     }
-    __syncthreads();
-    int slot = s_cnt[threadIdx.x], cp = s_ch[threadIdx.x], gp = s_gr[threadIdx.x];
+    int slot = cnt, cp = ch, gp = gr;
     for (int f = f0; f < f1; ++f)
         if (ld_vol(&C.fs[f].state) != ST_DONE) {
             C.active[slot] = f;
@@ -552,10 +567,14 @@ __device__ void r_step(const d2ic_frame_t *frames, int n_frames, Ctl &C, int eva
 template <int KIND>
 __global__ void __launch_bounds__(NG, 2) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
                                                    char *ctl_base, int eval_only, const float *u_eval,
-                                                   double *J_out, float *grad_out) {
+                                                   double *J_out, float *grad_out, unsigned long long *trace,
+                                                   int trace_rounds) {
     __shared__ double red[5][NWARP];
     Ctl C = make_ctl(ctl_base, n_frames);
     const int lane = threadIdx.x & 31;
+    // optional phase trace (block 0): [round start, after P barrier, end of own N, after R barrier]
+    const bool tr = trace != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
+    int round = 0;
 
     // ---- init: u <- u0, zero g/d buffers, NaN history ----
     for (int f = 0; f < n_frames; ++f) {
@@ -576,6 +595,8 @@ __global__ void __launch_bounds__(NG, 2) cg_engine(const d2ic_frame_t *__restric
     while (true) {
         const int na = ld_vol(&C.h->n_active);
         if (na == 0) break;
+        const bool trr = tr && round < trace_rounds;
+        if (trr) trace[4 * round + 0] = gtimer();
         // ---- P phase ----
         {
             const int total = ld_vol(&C.h->total_chunks);
@@ -592,6 +613,7 @@ __global__ void __launch_bounds__(NG, 2) cg_engine(const d2ic_frame_t *__restric
             }
         }
         if (!grid_barrier(C.h, [] {})) break;
+        if (trr) trace[4 * round + 1] = gtimer();
         // ---- N phase ----
         {
             const int tg = ld_vol(&C.h->total_groups);
@@ -601,7 +623,10 @@ __global__ void __launch_bounds__(NG, 2) cg_engine(const d2ic_frame_t *__restric
                 node_group(frames[f], C.fs + f, gi - __ldcg(C.gpre + s), red);
             }
         }
+        if (trr) trace[4 * round + 2] = gtimer();
         if (!grid_barrier(C.h, [&] { r_step(frames, n_frames, C, eval_only); })) break;
+        if (trr) trace[4 * round + 3] = gtimer();
+        ++round;
     }
 
 finish:
@@ -662,7 +687,7 @@ static int dev_info(int dev, DevInfo **out) {
 
 static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes, int kind,
                          int grid_blocks, int eval_only, const float *u_eval, double *J_out, float *grad_out,
-                         cudaStream_t s) {
+                         unsigned long long *trace, int trace_rounds, cudaStream_t s) {
     D2IC_REQUIRE(frames && control, "cg engine: null pointer");
     D2IC_REQUIRE(n_frames >= 1 && n_frames <= D2IC_MAX_FRAMES, "cg engine: n_frames %d out of [1, %d]", n_frames,
                  D2IC_MAX_FRAMES);
@@ -683,7 +708,7 @@ static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control
     if (e != cudaSuccess) return cuda_status(e, "control reset");
     char *cb = (char *)control;
     void *args[] = {(void *)&frames, (void *)&n_frames, (void *)&cb, (void *)&eval_only, (void *)&u_eval,
-                    (void *)&J_out, (void *)&grad_out};
+                    (void *)&J_out, (void *)&grad_out, (void *)&trace, (void *)&trace_rounds};
     if (kind == D2IC_INTERP_CUBIC)
         e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_CUBIC>, dim3(blocks), dim3(NG), args, 0, s);
     else
@@ -740,12 +765,20 @@ extern "C" int d2ic_device_info(int device, int *num_sms, int *engine_blocks_per
 extern "C" int d2ic_cg_solve_batched(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
                                      int interp_kind, int grid_blocks, void *stream) {
     return launch_engine(frames, n_frames, control, control_bytes, interp_kind, grid_blocks, 0, nullptr, nullptr,
-                         nullptr, (cudaStream_t)stream);
+                         nullptr, nullptr, 0, (cudaStream_t)stream);
+}
+
+extern "C" int d2ic_cg_solve_traced(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
+                                    int interp_kind, int grid_blocks, unsigned long long *trace, int trace_rounds,
+                                    void *stream) {
+    D2IC_REQUIRE(trace && trace_rounds > 0, "d2ic_cg_solve_traced: need a trace buffer");
+    return launch_engine(frames, n_frames, control, control_bytes, interp_kind, grid_blocks, 0, nullptr, nullptr,
+                         nullptr, trace, trace_rounds, (cudaStream_t)stream);
 }
 
 extern "C" int d2ic_eval_objective(const d2ic_frame_t *frame, const float *u, void *control, size_t control_bytes,
                                    int interp_kind, double *J_out, float *grad_out, void *stream) {
     D2IC_REQUIRE(u && J_out && grad_out, "d2ic_eval_objective: null pointer");
-    return launch_engine(frame, 1, control, control_bytes, interp_kind, 0, 1, u, J_out, grad_out,
+    return launch_engine(frame, 1, control, control_bytes, interp_kind, 0, 1, u, J_out, grad_out, nullptr, 0,
                          (cudaStream_t)stream);
 }

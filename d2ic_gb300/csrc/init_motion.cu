@@ -128,7 +128,10 @@ __global__ void zncc_kernel(const float *__restrict__ ref, int Hr, int Wr, const
     }
 }
 
-// IDW (power p) of centre displacements onto nodes, FP64 accumulation.
+// IDW (power p) of centre displacements onto nodes.  FP64 sqrt/divide are
+// slow on GB300, so per-pair math is FP32 (squared distances of pixel-grid
+// coordinates are exact in FP32 up to 2^24) with Kahan-compensated FP32 sums
+// inside each 256-centre tile and FP64 accumulation across tiles.
 __global__ void idw_kernel(const float2 *__restrict__ nodes, int n_nodes, const float2 *__restrict__ centers,
                            const float2 *__restrict__ disp, int nc, float power, float2 *__restrict__ out) {
     __shared__ float2 sc[256], sd[256];
@@ -137,6 +140,7 @@ __global__ void idw_kernel(const float2 *__restrict__ nodes, int n_nodes, const 
     double sw = 0.0, sx = 0.0, sy = 0.0;
     int exact = -1;
     float2 ev = make_float2(0.f, 0.f);
+    const bool p2 = (power == 2.0f);
     for (int base = 0; base < nc; base += 256) {
         const int m = min(256, nc - base);
         __syncthreads();
@@ -146,21 +150,27 @@ __global__ void idw_kernel(const float2 *__restrict__ nodes, int n_nodes, const 
         }
         __syncthreads();
         if (i < n_nodes && exact < 0) {
+            float tw = 0.f, tx = 0.f, ty = 0.f, cw = 0.f, cx = 0.f, cy = 0.f;   // tile sums + compensation
             for (int k = 0; k < m; ++k) {
                 const float2 d = sd[k];
                 if (d.x != d.x || d.y != d.y) continue;      // centres with NaN displacement are dropped
-                const double dx = (double)sc[k].x - p.x, dy = (double)sc[k].y - p.y;
-                const double dist = sqrt(dx * dx + dy * dy);
-                if (dist < 1e-6) {
+                const float dx = sc[k].x - p.x, dy = sc[k].y - p.y;
+                const float d2 = dx * dx + dy * dy;
+                if (d2 < 1e-12f) {                            // dist < 1e-6: take this centre's value
                     exact = base + k;
                     ev = d;
                     break;
                 }
-                const double w = (power == 2.0f) ? 1.0 / ((dist + 1e-12) * (dist + 1e-12)) : pow(dist + 1e-12, -(double)power);
-                sw += w;
-                sx += w * d.x;
-                sy += w * d.y;
+                const float w = p2 ? 1.0f / d2 : powf(sqrtf(d2), -power);
+                float y = w - cw, t = tw + y;
+                cw = (t - tw) - y;
+                tw = t;
+                y = w * d.x - cx; t = tx + y; cx = (t - tx) - y; tx = t;
+                y = w * d.y - cy; t = ty + y; cy = (t - ty) - y; ty = t;
             }
+            sw += (double)tw - (double)cw;
+            sx += (double)tx - (double)cx;
+            sy += (double)ty - (double)cy;
         }
     }
     if (i >= n_nodes) return;

@@ -140,6 +140,14 @@ D2IC_API size_t d2ic_cg_control_bytes(int n_frames);
 D2IC_API int d2ic_cg_solve_batched(const d2ic_frame_t *frames, int n_frames, void *control,
                           size_t control_bytes, int interp_kind, int grid_blocks, void *stream);
 
+/* As d2ic_cg_solve_batched, and block 0 writes 4 %globaltimer stamps per round
+ * (round start, after the pixel-pass barrier, end of its node pass, after the
+ * control barrier) into trace[4*r .. 4*r+3] for r < trace_rounds (diagnostics;
+ * no counterpart in the reference). */
+D2IC_API int d2ic_cg_solve_traced(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
+                                  int interp_kind, int grid_blocks, unsigned long long *trace, int trace_rounds,
+                                  void *stream);
+
 /* Objective and gradient at u for one frame (the value_and_grad of J_total,
  * d2ic/solver_global_cg.py:323).  frame: device pointer; control: as above for
  * one frame.  Writes J (1 double) and grad (2*n_nodes floats). */
