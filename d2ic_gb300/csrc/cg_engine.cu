@@ -40,6 +40,9 @@ namespace d2ic {
 
 constexpr int NG = D2IC_NODE_GROUP;            // threads per block == nodes per group
 constexpr int NWARP = NG / 32;
+#ifndef D2IC_ENGINE_MINB
+#define D2IC_ENGINE_MINB 2   // resident blocks per SM the register budget is sized for
+#endif
 constexpr unsigned long long WAIT_NS = 5ull * 1000ull * 1000ull * 1000ull;
 
 enum { ST_EVAL = 0, ST_TRIAL = 1, ST_FORCED = 2, ST_DONE = 3 };
@@ -294,28 +297,64 @@ __device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameSta
     const int igt = ld_vol(&S->igt), igc = ld_vol(&S->igc), iu = ld_vol(&S->iu), idp = ld_vol(&S->idp);
     double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     if (n < F.n_nodes) {
+        // All loads of a batch are issued before any is consumed: the node pass
+        // is a short chain of L2 round trips instead of one per table entry.
+        // Sums still run in table order.
+        constexpr int NB = 4;
         float2 dir;
         const float2 ui = cd.at(n, dir);
         float sx = 0.f, sy = 0.f;
         const int e0 = __ldg(F.node_chunk_ptr + n), e1 = __ldg(F.node_chunk_ptr + n + 1);
-        for (int e = e0; e < e1; ++e) {
-            const int ent = __ldg(F.node_chunk_ent + e);
-            const float *cgp = F.chunk_grad + 8 * (size_t)(ent >> 2) + (ent & 3);
-            sx += __ldcg(cgp);
-            sy += __ldcg(cgp + 4);
+        for (int eb = e0; eb < e1; eb += NB) {
+            int ent[NB];
+#pragma unroll
+            for (int q = 0; q < NB; ++q) ent[q] = (eb + q < e1) ? __ldg(F.node_chunk_ent + eb + q) : -1;
+            float vx[NB], vy[NB];
+#pragma unroll
+            for (int q = 0; q < NB; ++q) {
+                vx[q] = vy[q] = 0.f;
+                if (ent[q] >= 0) {
+                    const float *cgp = F.chunk_grad + 8 * (size_t)(ent[q] >> 2) + (ent[q] & 3);
+                    vx[q] = __ldcg(cgp);
+                    vy[q] = __ldcg(cgp + 4);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < NB; ++q)
+                if (ent[q] >= 0) {
+                    sx += vx[q];
+                    sy += vy[q];
+                }
         }
         float rx = 0.f, ry = 0.f, en = 0.f;
         const int md = F.max_deg;
-        for (int k = 0; k < md; ++k) {
-            const int j = __ldg(F.nbr_index + (size_t)n * md + k);
-            if (j < 0) break;
-            const float w = __ldg(F.nbr_weight + (size_t)n * md + k);
-            float2 dj;
-            const float2 uj = cd.at(j, dj);
-            const float ddx = ui.x - uj.x, ddy = ui.y - uj.y;
-            rx += w * ddx;
-            ry += w * ddy;
-            en += w * (ddx * ddx + ddy * ddy);
+        const int *nbi = F.nbr_index + (size_t)n * md;
+        const float *nbw = F.nbr_weight + (size_t)n * md;
+        bool alive = true;                               // entries after the first -1 are padding
+        for (int kb = 0; kb < md && alive; kb += NB) {
+            int jj[NB];
+            float ww[NB];
+#pragma unroll
+            for (int q = 0; q < NB; ++q) {
+                jj[q] = (kb + q < md) ? __ldg(nbi + kb + q) : -1;
+                ww[q] = (kb + q < md) ? __ldg(nbw + kb + q) : 0.f;
+            }
+            float2 uj[NB];
+#pragma unroll
+            for (int q = 0; q < NB; ++q) {
+                float2 dj;
+                uj[q] = (jj[q] >= 0) ? cd.at(jj[q], dj) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int q = 0; q < NB; ++q) {
+                alive = alive && jj[q] >= 0;
+                if (alive) {
+                    const float ddx = ui.x - uj[q].x, ddy = ui.y - uj[q].y;
+                    rx += ww[q] * ddx;
+                    ry += ww[q] * ddy;
+                    en += ww[q] * (ddx * ddx + ddy * ddy);
+                }
+            }
         }
         const float inv_np = 1.0f / (float)max(F.n_pix, 1);
         const float gx = sx * inv_np + F.alpha_reg * rx;
@@ -565,14 +604,15 @@ __device__ void r_step(const d2ic_frame_t *frames, int n_frames, Ctl &C, int eva
 // the persistent kernel
 // ---------------------------------------------------------------------------
 template <int KIND>
-__global__ void __launch_bounds__(NG, 2) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
+__global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
                                                    char *ctl_base, int eval_only, const float *u_eval,
                                                    double *J_out, float *grad_out, unsigned long long *trace,
                                                    int trace_rounds) {
     __shared__ double red[5][NWARP];
     Ctl C = make_ctl(ctl_base, n_frames);
     const int lane = threadIdx.x & 31;
-    // optional phase trace (block 0): [round start, after P barrier, end of own N, after R barrier]
+    // optional phase trace: block 0 stamps [round start, after P barrier, end of its N, -, -, after R
+    // barrier]; the last block stamps the start and end of its R step into slots 3 and 4
     const bool tr = trace != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
     int round = 0;
 
@@ -596,24 +636,29 @@ __global__ void __launch_bounds__(NG, 2) cg_engine(const d2ic_frame_t *__restric
         const int na = ld_vol(&C.h->n_active);
         if (na == 0) break;
         const bool trr = tr && round < trace_rounds;
-        if (trr) trace[4 * round + 0] = gtimer();
-        // ---- P phase ----
+        if (trr) trace[6 * round + 0] = gtimer();
+        // ---- P phase: chunk c of the active list goes to global warp c mod (warps in grid) ----
         {
             const int total = ld_vol(&C.h->total_chunks);
-            while (true) {
-                int c = 0;
-                if (lane == 0) c = (int)atomicAdd(&C.h->work, 1u);
-                c = __shfl_sync(0xffffffffu, c, 0);
-                if (c >= total) break;
-                const int s = find_slot(C.cpre, na, c);
-                const int f = __ldcg(C.active + s);
-                const d2ic_frame_t &F = frames[f];
-                const Cand cd = make_cand(F, C.fs + f);
-                pixel_chunk<KIND>(F, cd, c - __ldcg(C.cpre + s), lane);
+            const int gw = (int)((blockIdx.x * NG + threadIdx.x) >> 5);
+            const int nw = (int)((gridDim.x * NG) >> 5);
+            int cbase = 0, cend = 0;
+            const d2ic_frame_t *Fp = frames;
+            Cand cd;
+            for (int c = gw; c < total; c += nw) {
+                if (c >= cend) {                      // chunks ascend per warp: frames change forward only
+                    const int s = find_slot(C.cpre, na, c);
+                    const int f = __ldcg(C.active + s);
+                    cbase = __ldcg(C.cpre + s);
+                    cend = __ldcg(C.cpre + s + 1);
+                    Fp = frames + f;
+                    cd = make_cand(*Fp, C.fs + f);
+                }
+                pixel_chunk<KIND>(*Fp, cd, c - cbase, lane);
             }
         }
         if (!grid_barrier(C.h, [] {})) break;
-        if (trr) trace[4 * round + 1] = gtimer();
+        if (trr) trace[6 * round + 1] = gtimer();
         // ---- N phase ----
         {
             const int tg = ld_vol(&C.h->total_groups);
@@ -623,9 +668,15 @@ __global__ void __launch_bounds__(NG, 2) cg_engine(const d2ic_frame_t *__restric
                 node_group(frames[f], C.fs + f, gi - __ldcg(C.gpre + s), red);
             }
         }
-        if (trr) trace[4 * round + 2] = gtimer();
-        if (!grid_barrier(C.h, [&] { r_step(frames, n_frames, C, eval_only); })) break;
-        if (trr) trace[4 * round + 3] = gtimer();
+        if (trr) trace[6 * round + 2] = gtimer();
+        if (!grid_barrier(C.h, [&] {
+                const bool rt = trace != nullptr && threadIdx.x == 0 && round < trace_rounds;
+                if (rt) trace[6 * round + 3] = gtimer();
+                r_step(frames, n_frames, C, eval_only);
+                if (rt) trace[6 * round + 4] = gtimer();
+            }))
+            break;
+        if (trr) trace[6 * round + 5] = gtimer();
         ++round;
     }
 

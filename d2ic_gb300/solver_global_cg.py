@@ -44,7 +44,7 @@ class GlobalCGSolver(SolverBase):
     """Global CG solver for mesh DIC; expects ``MeshAssets.pixel_data``."""
 
     def __init__(self, verbose: bool = False, interpolation: str = "cubic", use_map_coordinates: bool | None = None,
-                 log_cg: bool = False, device=None, grid_blocks: int = 0) -> None:
+                 log_cg: bool = False, device=None, grid_blocks: int = 0, chunk_pixels: int = 256) -> None:
         self._compiled = False
         self._verbose = bool(verbose)
         self._log_cg = bool(log_cg)
@@ -56,6 +56,7 @@ class GlobalCGSolver(SolverBase):
         self._kind = interp_kind(self._interpolation)
         self._device = torch.device(device if device is not None else "cuda")
         self._grid_blocks = int(grid_blocks)
+        self._chunk_pixels = int(chunk_pixels)
         self._layout = None
         self._layout_key = None
         self._slot = None
@@ -77,7 +78,8 @@ class GlobalCGSolver(SolverBase):
         key = (id(pix), id(state.ref_image), int(state.config.max_iters))
         if self._layout is None or self._layout_key != key:
             n_nodes = int(np.asarray(assets.mesh.nodes_xy).shape[0])
-            self._layout = FrameLayout(pix, n_nodes, state.ref_image, self._interpolation, self._device)
+            self._layout = FrameLayout(pix, n_nodes, state.ref_image, self._interpolation, self._device,
+                                       chunk_max=self._chunk_pixels)
             self._slot = FrameSlot(self._layout, int(state.config.max_iters))
             self._engine = Engine(self._device, 1)
             self._layout_key = key

@@ -140,10 +140,11 @@ D2IC_API size_t d2ic_cg_control_bytes(int n_frames);
 D2IC_API int d2ic_cg_solve_batched(const d2ic_frame_t *frames, int n_frames, void *control,
                           size_t control_bytes, int interp_kind, int grid_blocks, void *stream);
 
-/* As d2ic_cg_solve_batched, and block 0 writes 4 %globaltimer stamps per round
- * (round start, after the pixel-pass barrier, end of its node pass, after the
- * control barrier) into trace[4*r .. 4*r+3] for r < trace_rounds (diagnostics;
- * no counterpart in the reference). */
+/* As d2ic_cg_solve_batched, and writes 6 %globaltimer stamps per round into
+ * trace[6*r .. 6*r+5] for r < trace_rounds: block 0's round start, end of the
+ * pixel-pass barrier and end of its node pass; start and end of the control
+ * step (by the block that ran it); block 0's exit from the control barrier
+ * (diagnostics; no counterpart in the reference). */
 D2IC_API int d2ic_cg_solve_traced(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
                                   int interp_kind, int grid_blocks, unsigned long long *trace, int trace_rounds,
                                   void *stream);
