@@ -46,13 +46,14 @@ class Frame(ctypes.Structure):
     """Mirror of ``d2ic_frame_t``."""
     _fields_ = [
         ("coeff", vp), ("pix", vp), ("chunk_begin", vp), ("chunk_nodes", vp),
-        ("node_chunk_ptr", vp), ("node_chunk_ent", vp), ("nbr_index", vp), ("nbr_weight", vp),
+        ("chunk_box", vp), ("node_chunk_ent", vp), ("nbr_index", vp), ("nbr_weight", vp),
         ("u0", vp), ("u_out", vp), ("hist", vp), ("n_iters", vp), ("status", vp), ("n_evals", vp),
         ("node_ws", vp), ("chunk_J", vp), ("chunk_grad", vp), ("group_part", vp),
         ("tol", f64), ("alpha_reg", f32), ("max_iter", i32),
         ("W", i32), ("H", i32), ("cpitch", i32), ("pad", i32),
         ("n_pix", i32), ("n_chunks", i32), ("n_nodes", i32), ("max_deg", i32),
         ("n_groups", i32), ("chunks_per_group", i32),
+        ("node_chunk_k", i32), ("reserved_", i32),
     ]
 
 

@@ -41,7 +41,7 @@ namespace d2ic {
 constexpr int NG = D2IC_NODE_GROUP;            // threads per block == nodes per group
 constexpr int NWARP = NG / 32;
 #ifndef D2IC_ENGINE_MINB
-#define D2IC_ENGINE_MINB 2   // resident blocks per SM the register budget is sized for
+#define D2IC_ENGINE_MINB 1   // resident blocks per SM the register budget is sized for
 #endif
 constexpr unsigned long long WAIT_NS = 5ull * 1000ull * 1000ull * 1000ull;
 
@@ -231,9 +231,26 @@ __device__ __forceinline__ int find_slot(const int *pre, int n, int x) {
 // ---------------------------------------------------------------------------
 // P phase: one chunk per warp
 // ---------------------------------------------------------------------------
+constexpr int RPL = D2IC_CHUNK_MAX / 32;      // pixel records per lane, prefetched together
+constexpr int TILE_CAP = 1024;                // floats of the per-warp coefficient tile
+
+// Since the Q4 weights of a pixel inside its element are a convex combination,
+// every displaced pixel of a chunk lies in the chunk's pixel box shifted by
+// [min_a u_a, max_a u_a]; that box plus the cubic stencil and one pixel of
+// margin is staged in shared memory once per chunk.  A chunk whose tile would
+// not fit, or a pixel that lands outside it, reads global memory instead; both
+// paths feed the same tap arithmetic.
 template <int KIND>
-__device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &cd, int c, int lane) {
+__device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &cd, int c, int lane, float *tile) {
     const int pb = __ldg(F.chunk_begin + c), pe = __ldg(F.chunk_begin + c + 1);
+    const int2 box = __ldg(reinterpret_cast<const int2 *>(F.chunk_box) + c);
+    const uint4 *pix = reinterpret_cast<const uint4 *>(F.pix);
+    uint4 rec[RPL];
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+        const int p = pb + lane + 32 * i;
+        rec[i] = (p < pe) ? __ldg(pix + p) : make_uint4(0u, 0u, 0u, 0u);
+    }
     float2 uc = make_float2(0.f, 0.f);
     if (lane < 4) {
         const int nd = __ldg(F.chunk_nodes + 4 * c + lane);
@@ -247,13 +264,34 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
         uy[a] = __shfl_sync(0xffffffffu, uc.y, a);
     }
     const Img im{F.coeff, F.W, F.H, F.cpitch, F.pad};
-    const uint4 *pix = reinterpret_cast<const uint4 *>(F.pix);
+    int tx0 = 0, ty0 = 0, tw = 0, th = 0;
+    bool use_tile = false;
+    if (KIND == D2IC_INTERP_CUBIC) {
+        const float mnx = fminf(fminf(ux[0], ux[1]), fminf(ux[2], ux[3]));
+        const float mxx = fmaxf(fmaxf(ux[0], ux[1]), fmaxf(ux[2], ux[3]));
+        const float mny = fminf(fminf(uy[0], uy[1]), fminf(uy[2], uy[3]));
+        const float mxy = fmaxf(fmaxf(uy[0], uy[1]), fmaxf(uy[2], uy[3]));
+        const int bx0 = box.x & 0xffff, by0 = (int)((unsigned)box.x >> 16);
+        const int bx1 = box.y & 0xffff, by1 = (int)((unsigned)box.y >> 16);
+        tx0 = bx0 + (int)safe_floor(mnx) - 2;
+        ty0 = by0 + (int)safe_floor(mny) - 2;
+        tw = bx1 + (int)safe_floor(mxx) + 3 - tx0 + 1;
+        th = by1 + (int)safe_floor(mxy) + 3 - ty0 + 1;
+        use_tile = tw >= 4 && th >= 4 && tw <= TILE_CAP && tw * th <= TILE_CAP;
+        if (use_tile) {
+            const int n = tw * th;
+            for (int i = lane; i < n; i += 32) {
+                const int ly = i / tw, lx = i - ly * tw;
+                tile[i] = im.at(clampi(ty0 + ly, -im.pad, im.H - 1 + im.pad), clampi(tx0 + lx, -im.pad, im.W - 1 + im.pad));
+            }
+            __syncwarp();
+        }
+    }
     float jr = 0.f;
     float gxa[4] = {0.f, 0.f, 0.f, 0.f}, gya[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int p = pb + lane; p < pe; p += 32) {
-        const uint4 rec = __ldg(pix + p);
-        const int x = (int)(rec.x & 0xffffu), y = (int)(rec.x >> 16);
-        const float I1 = __uint_as_float(rec.y), xi = __uint_as_float(rec.z), eta = __uint_as_float(rec.w);
+    auto one = [&](const uint4 r4) {
+        const int x = (int)(r4.x & 0xffffu), y = (int)(r4.x >> 16);
+        const float I1 = __uint_as_float(r4.y), xi = __uint_as_float(r4.z), eta = __uint_as_float(r4.w);
         const float a0 = 0.5f * (1.f - xi), a1 = 0.5f * (1.f + xi);
         const float b0 = 0.5f * (1.f - eta), b1 = 0.5f * (1.f + eta);
         const float N[4] = {a0 * b0, a1 * b0, a1 * b1, a0 * b1};
@@ -263,8 +301,12 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
         float tx, ty;
         split_coord(x, dx, ix, tx);
         split_coord(y, dy, iy, ty);
-        float gx, gy;
-        const float v = sample<KIND>(im, ix, iy, tx, ty, gx, gy);
+        float gx, gy, v;
+        const int lx = ix - 1 - tx0, ly = iy - 1 - ty0;
+        if (use_tile && lx >= 0 && ly >= 0 && lx <= tw - 4 && ly <= th - 4)
+            v = sample_cubic_tile(tile, tw, lx, ly, tx, ty, gx, gy);
+        else
+            v = sample<KIND>(im, ix, iy, tx, ty, gx, gy);
         const float r = v - I1;
         jr += r * r;
         const float rgx = r * gx, rgy = r * gy;
@@ -273,7 +315,11 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
             gxa[a] += rgx * N[a];
             gya[a] += rgy * N[a];
         }
-    }
+    };
+#pragma unroll
+    for (int i = 0; i < RPL; ++i)
+        if (pb + lane + 32 * i < pe) one(rec[i]);
+    for (int p = pb + lane + 32 * RPL; p < pe; p += 32) one(__ldg(pix + p));   // chunks longer than the prefetch
     const double js = warp_sum_d((double)jr);
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -286,6 +332,7 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
         cg[0] = make_float4(gxa[0], gxa[1], gxa[2], gxa[3]);
         cg[1] = make_float4(gya[0], gya[1], gya[2], gya[3]);
     }
+    __syncwarp();                                   // the tile is reused by the warp's next chunk
 }
 
 // ---------------------------------------------------------------------------
@@ -304,11 +351,11 @@ __device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameSta
         float2 dir;
         const float2 ui = cd.at(n, dir);
         float sx = 0.f, sy = 0.f;
-        const int e0 = __ldg(F.node_chunk_ptr + n), e1 = __ldg(F.node_chunk_ptr + n + 1);
-        for (int eb = e0; eb < e1; eb += NB) {
+        const int K = F.node_chunk_k, Nn = F.n_nodes;
+        for (int eb = 0; eb < K; eb += NB) {
             int ent[NB];
 #pragma unroll
-            for (int q = 0; q < NB; ++q) ent[q] = (eb + q < e1) ? __ldg(F.node_chunk_ent + eb + q) : -1;
+            for (int q = 0; q < NB; ++q) ent[q] = (eb + q < K) ? __ldg(F.node_chunk_ent + (size_t)(eb + q) * Nn + n) : -1;
             float vx[NB], vy[NB];
 #pragma unroll
             for (int q = 0; q < NB; ++q) {
@@ -328,16 +375,16 @@ __device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameSta
         }
         float rx = 0.f, ry = 0.f, en = 0.f;
         const int md = F.max_deg;
-        const int *nbi = F.nbr_index + (size_t)n * md;
-        const float *nbw = F.nbr_weight + (size_t)n * md;
+        const int *nbi = F.nbr_index + n;             // column-major: entry k at k * n_nodes
+        const float *nbw = F.nbr_weight + n;
         bool alive = true;                               // entries after the first -1 are padding
         for (int kb = 0; kb < md && alive; kb += NB) {
             int jj[NB];
             float ww[NB];
 #pragma unroll
             for (int q = 0; q < NB; ++q) {
-                jj[q] = (kb + q < md) ? __ldg(nbi + kb + q) : -1;
-                ww[q] = (kb + q < md) ? __ldg(nbw + kb + q) : 0.f;
+                jj[q] = (kb + q < md) ? __ldg(nbi + (size_t)(kb + q) * Nn) : -1;
+                ww[q] = (kb + q < md) ? __ldg(nbw + (size_t)(kb + q) * Nn) : 0.f;
             }
             float2 uj[NB];
 #pragma unroll
@@ -577,11 +624,16 @@ __device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
 }
 
 __device__ void r_step(const d2ic_frame_t *frames, int n_frames, Ctl &C, int eval_only) {
+    __shared__ int s_finished;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_finished = 0;
+    __syncthreads();
     const int na = ld_vol(&C.h->n_active);
     for (int s = wid; s < na; s += NWARP) {
         const int f = ld_vol(C.active + s);
         const d2ic_frame_t &F = frames[f];
+        FrameState S;
+        if (lane == 0) S = load_fs(C.fs + f);          // issued together with the partial loads below
         double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
         for (int g = lane; g < F.n_groups; g += 32) {
 #pragma unroll
@@ -590,14 +642,21 @@ __device__ void r_step(const d2ic_frame_t *frames, int n_frames, Ctl &C, int eva
 #pragma unroll
         for (int i = 0; i < 5; ++i) q[i] = warp_sum_d(q[i]);
         if (lane == 0) {
-            FrameState S = load_fs(C.fs + f);
             frame_decide(S, F, q, eval_only);
             C.fs[f] = S;
+            if (S.state == ST_DONE) s_finished = 1;
         }
     }
-    __threadfence();
     __syncthreads();
-    rebuild_active(frames, n_frames, C);
+    if (s_finished) {
+        rebuild_active(frames, n_frames, C);
+    } else if (threadIdx.x == 0) {                     // active set unchanged: keep the lists
+        C.h->rounds += 1;
+        if (C.h->rounds > C.h->max_rounds) {
+            C.h->err = D2IC_MAX_ITERS;
+            C.h->abort = 1;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -609,6 +668,7 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                                                    double *J_out, float *grad_out, unsigned long long *trace,
                                                    int trace_rounds) {
     __shared__ double red[5][NWARP];
+    extern __shared__ float s_tile[];              // NWARP * TILE_CAP floats
     Ctl C = make_ctl(ctl_base, n_frames);
     const int lane = threadIdx.x & 31;
     // optional phase trace: block 0 stamps [round start, after P barrier, end of its N, -, -, after R
@@ -654,7 +714,7 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                     Fp = frames + f;
                     cd = make_cand(*Fp, C.fs + f);
                 }
-                pixel_chunk<KIND>(*Fp, cd, c - cbase, lane);
+                pixel_chunk<KIND>(*Fp, cd, c - cbase, lane, s_tile + (threadIdx.x >> 5) * TILE_CAP);
             }
         }
         if (!grid_barrier(C.h, [] {})) break;
@@ -708,9 +768,13 @@ finish:
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+constexpr size_t ENGINE_SMEM = sizeof(float) * NWARP * TILE_CAP;   // per-warp coefficient tiles
+
 template <int KIND>
 static cudaError_t occupancy(int *blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cg_engine<KIND>, NG, 0);
+    cudaError_t e = cudaFuncSetAttribute(cg_engine<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ENGINE_SMEM);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cg_engine<KIND>, NG, ENGINE_SMEM);
 }
 
 struct DevInfo {
@@ -761,9 +825,11 @@ static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control
     void *args[] = {(void *)&frames, (void *)&n_frames, (void *)&cb, (void *)&eval_only, (void *)&u_eval,
                     (void *)&J_out, (void *)&grad_out, (void *)&trace, (void *)&trace_rounds};
     if (kind == D2IC_INTERP_CUBIC)
-        e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_CUBIC>, dim3(blocks), dim3(NG), args, 0, s);
+        e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_CUBIC>, dim3(blocks), dim3(NG), args,
+                                        ENGINE_SMEM, s);
     else
-        e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_LINEAR>, dim3(blocks), dim3(NG), args, 0, s);
+        e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_LINEAR>, dim3(blocks), dim3(NG), args,
+                                        ENGINE_SMEM, s);
     if (e != cudaSuccess) return cuda_status(e, "cudaLaunchCooperativeKernel(cg_engine)");
     return D2IC_OK;
 }

@@ -51,28 +51,40 @@ struct Img {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
 
+// The 4x4 tap arithmetic of the cubic B-spline, shared by every source of
+// coefficients (global memory, clamped global, shared-memory tile) so that all
+// paths produce identical bits.  Taps c[a][b]: row iy - 1 + a, column ix - 1 + b.
+__device__ __forceinline__ float cubic_taps(const float c[4][4], float tx, float ty, float &gx, float &gy) {
+    float wx[4], dwx[4], wy[4], dwy[4];
+    bspline_w(tx, wx, dwx);
+    bspline_w(ty, wy, dwy);
+    float v = 0.f, ax = 0.f, ay = 0.f;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        const float rv = __fmaf_rn(wx[3], c[a][3], __fmaf_rn(wx[2], c[a][2], __fmaf_rn(wx[1], c[a][1], wx[0] * c[a][0])));
+        const float rd = __fmaf_rn(dwx[3], c[a][3], __fmaf_rn(dwx[2], c[a][2], __fmaf_rn(dwx[1], c[a][1], dwx[0] * c[a][0])));
+        v = __fmaf_rn(wy[a], rv, v);
+        ax = __fmaf_rn(wy[a], rd, ax);
+        ay = __fmaf_rn(dwy[a], rv, ay);
+    }
+    gx = ax;
+    gy = ay;
+    return v;
+}
+
 // Cubic B-spline value and gradient at pixel (ix + tx, iy + ty), with integer
 // base (ix, iy) and fractional parts tx, ty in [0, 1).  Taps outside the halo'd
 // array clamp to its border, where the coefficients equal the edge value.
 __device__ __forceinline__ float sample_cubic(const Img &im, int ix, int iy, float tx, float ty,
                                               float &gx, float &gy) {
-    float wx[4], dwx[4], wy[4], dwy[4];
-    bspline_w(tx, wx, dwx);
-    bspline_w(ty, wy, dwy);
-    float v = 0.f, ax = 0.f, ay = 0.f;
+    float c[4][4];
     const int x0 = ix - 1, y0 = iy - 1;
     if (x0 >= -im.pad && x0 + 3 < im.W + im.pad && y0 >= -im.pad && y0 + 3 < im.H + im.pad) {
         const float *base = im.c + (size_t)(y0 + im.pad) * im.cp + (x0 + im.pad);
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const float *row = base + (size_t)a * im.cp;
-            const float c0 = __ldg(row), c1 = __ldg(row + 1), c2 = __ldg(row + 2), c3 = __ldg(row + 3);
-            const float rv = wx[0] * c0 + wx[1] * c1 + wx[2] * c2 + wx[3] * c3;
-            const float rd = dwx[0] * c0 + dwx[1] * c1 + dwx[2] * c2 + dwx[3] * c3;
-            v += wy[a] * rv;
-            ax += wy[a] * rd;
-            ay += dwy[a] * rv;
-        }
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) c[a][b] = __ldg(base + (size_t)a * im.cp + b);
     } else {
         int cx[4];
 #pragma unroll
@@ -80,17 +92,25 @@ __device__ __forceinline__ float sample_cubic(const Img &im, int ix, int iy, flo
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int r = clampi(y0 + a, -im.pad, im.H - 1 + im.pad);
-            const float c0 = im.at(r, cx[0]), c1 = im.at(r, cx[1]), c2 = im.at(r, cx[2]), c3 = im.at(r, cx[3]);
-            const float rv = wx[0] * c0 + wx[1] * c1 + wx[2] * c2 + wx[3] * c3;
-            const float rd = dwx[0] * c0 + dwx[1] * c1 + dwx[2] * c2 + dwx[3] * c3;
-            v += wy[a] * rv;
-            ax += wy[a] * rd;
-            ay += dwy[a] * rv;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) c[a][b] = im.at(r, cx[b]);
         }
     }
-    gx = ax;
-    gy = ay;
-    return v;
+    return cubic_taps(c, tx, ty, gx, gy);
+}
+
+// Same, with the taps read from a shared-memory tile whose element (0, 0) is the
+// tap at (row ly, column lx) relative to the tile; the caller guarantees
+// 0 <= lx <= tw - 4 and 0 <= ly <= th - 4.
+__device__ __forceinline__ float sample_cubic_tile(const float *tile, int tw, int lx, int ly, float tx, float ty,
+                                                   float &gx, float &gy) {
+    float c[4][4];
+    const float *base = tile + ly * tw + lx;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) c[a][b] = base[a * tw + b];
+    return cubic_taps(c, tx, ty, gx, gy);
 }
 
 // Bilinear value and gradient at pixel (ix + tx, iy + ty); taps clamped into the image.

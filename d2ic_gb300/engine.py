@@ -9,10 +9,12 @@ Data layout in HBM (per reference image + mesh, built once by
   256 pixels;
 * ``chunk_begin`` (Nc+1), ``chunk_nodes`` (Nc, 4): chunk extents and the 4
   nodes of the chunk's element;
-* ``node_chunk_ptr`` / ``node_chunk_ent``: node -> (chunk, local slot) CSR,
-  the transpose of the chunk -> node gather (no atomics);
-* ``nbr_index`` / ``nbr_weight``: the spring table, weights pre-multiplied by
-  (rho_i + rho_j)/2 in FP32.
+* ``chunk_box`` (Nc, 2): inclusive pixel box of each chunk, which bounds the
+  chunk's shared-memory coefficient tile;
+* ``node_chunk_ent`` (K, Nn): node -> (chunk, local slot) table, the transpose
+  of the chunk -> node gather (no atomics), column-major, -1 padded;
+* ``nbr_index`` / ``nbr_weight`` (max_deg, Nn): the spring table, column-major,
+  weights pre-multiplied by (rho_i + rho_j)/2 in FP32.
 
 Per frame being solved (:class:`FrameSlot`): the deformed image's
 B-spline coefficients with a 16-pixel halo (row pitch a multiple of 32
@@ -111,6 +113,9 @@ class FrameLayout:
 
     def __init__(self, pix, n_nodes: int, ref_image, interpolation: str = "cubic", device=None,
                  chunk_max: int = _lib.CHUNK_MAX):
+        if not 1 <= int(chunk_max) <= _lib.CHUNK_MAX:
+            raise ValueError(f"chunk_max must be in [1, {_lib.CHUNK_MAX}]")
+        chunk_max = int(chunk_max)
         self.device = torch.device(device if device is not None else "cuda")
         self.kind = interp_kind(interpolation)
         self.n_nodes = int(n_nodes)
@@ -140,14 +145,29 @@ class FrameLayout:
             chunk_begin = np.zeros(1, np.int32)
             chunk_nodes = np.zeros((0, 4), np.int32)
         self.n_chunks = int(chunk_begin.size - 1)
-        # node -> (chunk, slot) CSR
+        # inclusive pixel box of each chunk (bounds of its shared-memory coefficient tile)
+        colrow = np.stack([np.floor(pc[:, 0] - 0.5), np.floor(pc[:, 1] - 0.5)], axis=1).astype(np.int64)[order]
+        if self.n_chunks:
+            cstart = chunk_begin[:-1].astype(np.int64)
+            bx0 = np.minimum.reduceat(colrow[:, 0], cstart)
+            by0 = np.minimum.reduceat(colrow[:, 1], cstart)
+            bx1 = np.maximum.reduceat(colrow[:, 0], cstart)
+            by1 = np.maximum.reduceat(colrow[:, 1], cstart)
+            chunk_box = np.stack([bx0 | (by0 << 16), bx1 | (by1 << 16)], axis=1).astype(np.int64)
+            chunk_box = chunk_box.astype(np.uint32).view(np.int32)
+        else:
+            chunk_box = np.zeros((0, 2), np.int32)
+        # node -> (chunk << 2 | slot) table, fixed width K, column-major, ascending chunk order
         flat = chunk_nodes.reshape(-1).astype(np.int64)
         ent = (np.repeat(np.arange(self.n_chunks, dtype=np.int64), 4) << 2) | np.tile(np.arange(4), self.n_chunks)
         o = np.argsort(flat, kind="stable")
         cnt = np.bincount(flat, minlength=self.n_nodes)
-        self.node_chunk_ptr_h = np.r_[0, np.cumsum(cnt)].astype(np.int32)
-        node_chunk_ent = ent[o].astype(np.int32)
-        # spring table: entries beyond the degree are padding
+        K = max(int(cnt.max(initial=0)), 1)
+        rank = np.arange(flat.size) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+        node_chunk_ent = -np.ones((K, self.n_nodes), dtype=np.int32)
+        node_chunk_ent[rank, flat[o]] = ent[o]
+        self.node_chunk_k = K
+        # spring table: entries beyond the degree are padding; column-major for coalesced node-pass loads
         nbi = np.asarray(pix.node_neighbor_index, dtype=np.int64).reshape(self.n_nodes, -1)
         md = nbi.shape[1]
         deg = np.asarray(pix.node_neighbor_degree, dtype=np.int64)
@@ -157,19 +177,19 @@ class FrameLayout:
         w = np.asarray(pix.node_neighbor_weight, dtype=np.float32).reshape(self.n_nodes, -1)
         wc = (w * np.float32(0.5) * (rho[:, None] + rho[nid])).astype(np.float32)
         self.max_deg = md
-        nbr_index = np.where(valid, nbi, -1).astype(np.int32)
-        nbr_weight = np.where(valid, wc, np.float32(0)).astype(np.float32)
+        nbr_index = np.where(valid, nbi, -1).astype(np.int32).T.copy()
+        nbr_weight = np.where(valid, wc, np.float32(0)).astype(np.float32).T.copy()
         # pixel records (I1 sampled on the device from the reference image)
-        colrow = np.stack([np.floor(pc[:, 0] - 0.5), np.floor(pc[:, 1] - 0.5)], axis=1).astype(np.int32)[order]
+        colrow = colrow.astype(np.int32)
         xieta = _xi_eta(pix).astype(np.float32)[order]
         dev = self.device
         T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
         self.chunk_begin = T(chunk_begin)
         self.chunk_nodes = T(chunk_nodes)
-        self.node_chunk_ptr = T(self.node_chunk_ptr_h)
+        self.chunk_box = T(chunk_box) if self.n_chunks else torch.zeros((1, 2), dtype=torch.int32, device=dev)
         self.node_chunk_ent = T(node_chunk_ent)
-        self.nbr_index = T(nbr_index)
-        self.nbr_weight = T(nbr_weight)
+        self.nbr_index = T(nbr_index) if md else torch.full((1,), -1, dtype=torch.int32, device=dev)
+        self.nbr_weight = T(nbr_weight) if md else torch.zeros((1,), dtype=torch.float32, device=dev)
         self.pixel_order = order
         self.pix = torch.empty((max(Np, 1), 4), dtype=torch.int32, device=dev)
         ref_coeff = prepare_coefficients(ref, self.kind)
@@ -210,8 +230,9 @@ class FrameSlot:
         f.pix = ptr(L.pix)
         f.chunk_begin = ptr(L.chunk_begin)
         f.chunk_nodes = ptr(L.chunk_nodes)
-        f.node_chunk_ptr = ptr(L.node_chunk_ptr)
+        f.chunk_box = ptr(L.chunk_box)
         f.node_chunk_ent = ptr(L.node_chunk_ent)
+        f.node_chunk_k = L.node_chunk_k
         f.nbr_index = ptr(L.nbr_index)
         f.nbr_weight = ptr(L.nbr_weight)
         f.u0 = ptr(self.u0)

@@ -68,10 +68,14 @@ typedef struct d2ic_frame {
     const d2ic_pixrec_t *pix;
     const int   *chunk_begin;      /* n_chunks + 1                                      */
     const int   *chunk_nodes;      /* 4 * n_chunks, the chunk's element nodes (Q4 order) */
-    const int   *node_chunk_ptr;   /* n_nodes + 1                                       */
-    const int   *node_chunk_ent;   /* (chunk << 2) | local node slot, by node           */
-    const int   *nbr_index;        /* n_nodes * max_deg spring neighbours, -1 padded    */
-    const float *nbr_weight;       /* w_ij * (rho_i + rho_j) / 2                        */
+    const int   *chunk_box;        /* 2 * n_chunks: (col0 | row0 << 16, col1 | row1 << 16),
+                                      inclusive pixel box of the chunk                  */
+    const int   *node_chunk_ent;   /* node_chunk_k * n_nodes, column-major (slot k of node
+                                      n at k * n_nodes + n): (chunk << 2) | local node
+                                      slot, in ascending chunk order, -1 padded           */
+    const int   *nbr_index;        /* max_deg * n_nodes spring neighbours, column-major,
+                                      -1 padded after the last neighbour                */
+    const float *nbr_weight;       /* same layout: w_ij * (rho_i + rho_j) / 2           */
     const float *u0;               /* 2 * n_nodes initial displacement                  */
     float       *u_out;            /* 2 * n_nodes solution                              */
     float       *hist;             /* 3 * max_iter CG history [J, |g|, alpha], NaN-filled */
@@ -89,6 +93,7 @@ typedef struct d2ic_frame {
     int          W, H, cpitch, pad;
     int          n_pix, n_chunks, n_nodes, max_deg;
     int          n_groups, chunks_per_group;
+    int          node_chunk_k, reserved_;
 } d2ic_frame_t;
 
 /* ---- library ------------------------------------------------------------- */
