@@ -43,6 +43,16 @@ constexpr int NWARP = NG / 32;
 #ifndef D2IC_ENGINE_MINB
 #define D2IC_ENGINE_MINB 1   // resident blocks per SM the register budget is sized for
 #endif
+// Staging each chunk's coefficient tile in shared memory measured slower than
+// reading the taps through L1 (each coefficient is reused by ~16 pixels of the
+// chunk, which L1 captures; the tile fill adds a dependent round trip per
+// chunk), so it is compiled out by default.
+#ifndef D2IC_ENGINE_TILE
+#define D2IC_ENGINE_TILE 0
+#endif
+#ifndef D2IC_ENGINE_RPL
+#define D2IC_ENGINE_RPL 8    // pixel records per lane prefetched at chunk start (<= 256 / 32)
+#endif
 constexpr unsigned long long WAIT_NS = 5ull * 1000ull * 1000ull * 1000ull;
 
 enum { ST_EVAL = 0, ST_TRIAL = 1, ST_FORCED = 2, ST_DONE = 3 };
@@ -163,14 +173,15 @@ struct Cand {
 
 __device__ __forceinline__ Cand make_cand(const d2ic_frame_t &F, const FrameState *S) {
     Cand c;
-    const int iu = ld_vol(&S->iu), igc = ld_vol(&S->igc), idp = ld_vol(&S->idp);
-    const int st = ld_vol(&S->state);
+    // L2 loads (not volatile) so that the eight reads are in flight together
+    const int iu = __ldcg(&S->iu), igc = __ldcg(&S->igc), idp = __ldcg(&S->idp);
+    const int st = __ldcg(&S->state);
     c.u = nbuf(F, iu);
     c.g = nbuf(F, 2 + igc);
     c.d = nbuf(F, 5 + idp);
-    c.alpha = *(volatile const float *)&S->alpha;
-    c.beta = *(volatile const float *)&S->beta;
-    const int k = ld_vol(&S->k), rs = ld_vol(&S->restart);
+    c.alpha = __ldcg(&S->alpha);
+    c.beta = __ldcg(&S->beta);
+    const int k = __ldcg(&S->k), rs = __ldcg(&S->restart);
     c.mode = (st == ST_EVAL) ? 0 : ((rs || k == 0) ? 2 : 1);
     return c;
 }
@@ -231,7 +242,7 @@ __device__ __forceinline__ int find_slot(const int *pre, int n, int x) {
 // ---------------------------------------------------------------------------
 // P phase: one chunk per warp
 // ---------------------------------------------------------------------------
-constexpr int RPL = D2IC_CHUNK_MAX / 32;      // pixel records per lane, prefetched together
+constexpr int RPL = D2IC_ENGINE_RPL;          // pixel records per lane, prefetched together
 constexpr int TILE_CAP = 1024;                // floats of the per-warp coefficient tile
 
 // Since the Q4 weights of a pixel inside its element are a convex combination,
@@ -245,7 +256,7 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
     const int pb = __ldg(F.chunk_begin + c), pe = __ldg(F.chunk_begin + c + 1);
     const int2 box = __ldg(reinterpret_cast<const int2 *>(F.chunk_box) + c);
     const uint4 *pix = reinterpret_cast<const uint4 *>(F.pix);
-    uint4 rec[RPL];
+    uint4 rec[RPL > 0 ? RPL : 1];
 #pragma unroll
     for (int i = 0; i < RPL; ++i) {
         const int p = pb + lane + 32 * i;
@@ -277,12 +288,15 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
         ty0 = by0 + (int)safe_floor(mny) - 2;
         tw = bx1 + (int)safe_floor(mxx) + 3 - tx0 + 1;
         th = by1 + (int)safe_floor(mxy) + 3 - ty0 + 1;
-        use_tile = tw >= 4 && th >= 4 && tw <= TILE_CAP && tw * th <= TILE_CAP;
+        use_tile = D2IC_ENGINE_TILE && tw >= 4 && th >= 4 && tw <= 64 && tw * th <= TILE_CAP;
         if (use_tile) {
-            const int n = tw * th;
-            for (int i = lane; i < n; i += 32) {
-                const int ly = i / tw, lx = i - ly * tw;
-                tile[i] = im.at(clampi(ty0 + ly, -im.pad, im.H - 1 + im.pad), clampi(tx0 + lx, -im.pad, im.W - 1 + im.pad));
+            // one tile row per warp instruction: lane -> column (two columns per lane when tw > 32)
+            const int c0 = clampi(tx0 + lane, -im.pad, im.W - 1 + im.pad) + im.pad;
+            const int c1 = clampi(tx0 + lane + 32, -im.pad, im.W - 1 + im.pad) + im.pad;
+            for (int ly = 0; ly < th; ++ly) {
+                const float *row = im.c + (size_t)(clampi(ty0 + ly, -im.pad, im.H - 1 + im.pad) + im.pad) * im.cp;
+                if (lane < tw) tile[ly * tw + lane] = __ldg(row + c0);
+                if (lane + 32 < tw) tile[ly * tw + lane + 32] = __ldg(row + c1);
             }
             __syncwarp();
         }
@@ -341,13 +355,14 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
 __device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameState *S, int g, double (*red)[NWARP]) {
     const Cand cd = make_cand(F, S);
     const int n = g * NG + threadIdx.x;
-    const int igt = ld_vol(&S->igt), igc = ld_vol(&S->igc), iu = ld_vol(&S->iu), idp = ld_vol(&S->idp);
+    const int igt = __ldcg(&S->igt), igc = __ldcg(&S->igc), iu = __ldcg(&S->iu), idp = __ldcg(&S->idp);
     double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     if (n < F.n_nodes) {
         // All loads of a batch are issued before any is consumed: the node pass
         // is a short chain of L2 round trips instead of one per table entry.
         // Sums still run in table order.
         constexpr int NB = 4;
+        const float2 gc = __ldcg(nbuf(F, 2 + igc) + n);  // issued with the candidate's own loads
         float2 dir;
         const float2 ui = cd.at(n, dir);
         float sx = 0.f, sy = 0.f;
@@ -378,22 +393,23 @@ __device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameSta
         const int *nbi = F.nbr_index + n;             // column-major: entry k at k * n_nodes
         const float *nbw = F.nbr_weight + n;
         bool alive = true;                               // entries after the first -1 are padding
-        for (int kb = 0; kb < md && alive; kb += NB) {
-            int jj[NB];
-            float ww[NB];
+        constexpr int NBN = 8;
+        for (int kb = 0; kb < md && alive; kb += NBN) {
+            int jj[NBN];
+            float ww[NBN];
 #pragma unroll
-            for (int q = 0; q < NB; ++q) {
+            for (int q = 0; q < NBN; ++q) {
                 jj[q] = (kb + q < md) ? __ldg(nbi + (size_t)(kb + q) * Nn) : -1;
                 ww[q] = (kb + q < md) ? __ldg(nbw + (size_t)(kb + q) * Nn) : 0.f;
             }
-            float2 uj[NB];
+            float2 uj[NBN];
 #pragma unroll
-            for (int q = 0; q < NB; ++q) {
+            for (int q = 0; q < NBN; ++q) {
                 float2 dj;
                 uj[q] = (jj[q] >= 0) ? cd.at(jj[q], dj) : make_float2(0.f, 0.f);
             }
 #pragma unroll
-            for (int q = 0; q < NB; ++q) {
+            for (int q = 0; q < NBN; ++q) {
                 alive = alive && jj[q] >= 0;
                 if (alive) {
                     const float ddx = ui.x - uj[q].x, ddy = ui.y - uj[q].y;
@@ -409,7 +425,6 @@ __device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameSta
         nbuf(F, 2 + igt)[n] = make_float2(gx, gy);
         nbuf(F, 1 - iu)[n] = ui;
         nbuf(F, 5 + (1 - idp))[n] = dir;
-        const float2 gc = __ldcg(nbuf(F, 2 + igc) + n);
         q[P_EREG] = 0.25 * (double)en;
         q[P_GG] = (double)gx * gx + (double)gy * gy;
         q[P_GDIFF] = (double)gx * ((double)gx - gc.x) + (double)gy * ((double)gy - gc.y);
@@ -672,7 +687,8 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     Ctl C = make_ctl(ctl_base, n_frames);
     const int lane = threadIdx.x & 31;
     // optional phase trace: block 0 stamps [round start, after P barrier, end of its N, -, -, after R
-    // barrier]; the last block stamps the start and end of its R step into slots 3 and 4
+    // barrier, end of its own P work]; the last block stamps the start and end of its R step into
+    // slots 3 and 4
     const bool tr = trace != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
     int round = 0;
 
@@ -696,7 +712,7 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         const int na = ld_vol(&C.h->n_active);
         if (na == 0) break;
         const bool trr = tr && round < trace_rounds;
-        if (trr) trace[6 * round + 0] = gtimer();
+        if (trr) trace[7 * round + 0] = gtimer();
         // ---- P phase: chunk c of the active list goes to global warp c mod (warps in grid) ----
         {
             const int total = ld_vol(&C.h->total_chunks);
@@ -717,8 +733,12 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 pixel_chunk<KIND>(*Fp, cd, c - cbase, lane, s_tile + (threadIdx.x >> 5) * TILE_CAP);
             }
         }
+        if (trace != nullptr && blockIdx.x == 0 && round < trace_rounds) {
+            __syncthreads();
+            if (threadIdx.x == 0) trace[7 * round + 6] = gtimer();
+        }
         if (!grid_barrier(C.h, [] {})) break;
-        if (trr) trace[6 * round + 1] = gtimer();
+        if (trr) trace[7 * round + 1] = gtimer();
         // ---- N phase ----
         {
             const int tg = ld_vol(&C.h->total_groups);
@@ -728,15 +748,15 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 node_group(frames[f], C.fs + f, gi - __ldcg(C.gpre + s), red);
             }
         }
-        if (trr) trace[6 * round + 2] = gtimer();
+        if (trr) trace[7 * round + 2] = gtimer();
         if (!grid_barrier(C.h, [&] {
                 const bool rt = trace != nullptr && threadIdx.x == 0 && round < trace_rounds;
-                if (rt) trace[6 * round + 3] = gtimer();
+                if (rt) trace[7 * round + 3] = gtimer();
                 r_step(frames, n_frames, C, eval_only);
-                if (rt) trace[6 * round + 4] = gtimer();
+                if (rt) trace[7 * round + 4] = gtimer();
             }))
             break;
-        if (trr) trace[6 * round + 5] = gtimer();
+        if (trr) trace[7 * round + 5] = gtimer();
         ++round;
     }
 
@@ -899,3 +919,4 @@ extern "C" int d2ic_eval_objective(const d2ic_frame_t *frame, const float *u, vo
     return launch_engine(frame, 1, control, control_bytes, interp_kind, 0, 1, u, J_out, grad_out, nullptr, 0,
                          (cudaStream_t)stream);
 }
+

@@ -290,15 +290,15 @@ class Engine:
                   grid_blocks, _lib.stream_handle(stream))
 
     def solve_traced(self, desc_dev: torch.Tensor, n_frames: int, kind: int, rounds: int = 4096, grid_blocks: int = 0):
-        """Solve; per-round durations in microseconds: pixel pass + barrier, block 0's node pass,
-        wait until the control step starts, control step, release after it."""
-        tr = torch.zeros(6 * rounds, dtype=torch.int64, device=self.device)
+        """Solve; per-round durations in microseconds: block 0's own pixel work, its wait at the
+        pixel-pass barrier, its node pass, wait until the control step starts, control step, release."""
+        tr = torch.zeros(7 * rounds, dtype=torch.int64, device=self.device)
         _lib.call("d2ic_cg_solve_traced", ptr(desc_dev), n_frames, ptr(self.control), self.control.numel(), kind,
                   grid_blocks, ptr(tr), rounds, _lib.stream_handle())
-        t = tr.cpu().numpy().reshape(-1, 6).astype(np.float64)
+        t = tr.cpu().numpy().reshape(-1, 7).astype(np.float64)
         t = t[t[:, 5] > 0]
-        return np.stack([t[:, 1] - t[:, 0], t[:, 2] - t[:, 1], t[:, 3] - t[:, 2], t[:, 4] - t[:, 3],
-                         t[:, 5] - t[:, 4]], axis=1) / 1e3
+        return np.stack([t[:, 6] - t[:, 0], t[:, 1] - t[:, 6], t[:, 2] - t[:, 1], t[:, 3] - t[:, 2],
+                         t[:, 4] - t[:, 3], t[:, 5] - t[:, 4]], axis=1) / 1e3
 
     def eval_objective(self, desc_dev: torch.Tensor, u: torch.Tensor, kind: int, stream=None):
         J = torch.zeros(1, dtype=torch.float64, device=self.device)
