@@ -70,6 +70,7 @@ _SIGS = {
     "d2ic_cg_control_bytes": (szt, [i32]),
     "d2ic_cg_solve_batched": (i32, [vp, i32, vp, szt, i32, i32, vp]),
     "d2ic_cg_solve_traced": (i32, [vp, i32, vp, szt, i32, i32, vp, i32, vp]),
+    "d2ic_cg_solve_noalloc": (i32, [vp, i32, vp]),
     "d2ic_eval_objective": (i32, [vp, vp, vp, szt, i32, vp, vp, vp]),
     "d2ic_zncc_match": (i32, [vp, i32, i32, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp]),
     "d2ic_idw_project": (i32, [vp, i32, vp, vp, i32, f32, vp, vp]),

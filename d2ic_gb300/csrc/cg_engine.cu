@@ -920,3 +920,48 @@ extern "C" int d2ic_eval_objective(const d2ic_frame_t *frame, const float *u, vo
                          (cudaStream_t)stream);
 }
 
+// ---------------------------------------------------------------------------
+// Solve without allocating: scratch in a fixed device array
+// ---------------------------------------------------------------------------
+// For callers that cannot call cudaMalloc (an allocator-less runtime, a
+// plugin host that owns all device memory, code running where allocation is
+// forbidden): the engine's scratch -- the frame descriptor copy, the control
+// block and the per-frame workspace -- is carved from this file-scope device
+// array instead of caller memory.  Every GPU that loads the library holds the
+// array until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[D2IC_NOALLOC_SCRATCH_BYTES];
+static void *g_noalloc_addr[64];   // device address of the array, per device (host-side stand-in is not usable)
+
+extern "C" int d2ic_cg_solve_noalloc(const d2ic_frame_t *frame, int interp_kind, void *stream) {
+    D2IC_REQUIRE(frame, "d2ic_cg_solve_noalloc: null frame");
+    D2IC_REQUIRE(frame->n_nodes >= 1 && frame->n_chunks >= 0, "d2ic_cg_solve_noalloc: bad sizes");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+    D2IC_REQUIRE(dev >= 0 && dev < 64, "d2ic_cg_solve_noalloc: device index %d out of range", dev);
+    const size_t desc_bytes = align256(sizeof(d2ic_frame_t));
+    const size_t ctl_bytes = d2ic_cg_control_bytes(1);
+    const size_t ws_bytes = d2ic_frame_workspace_bytes(frame->n_nodes, frame->n_chunks);
+    const size_t need = desc_bytes + ctl_bytes + ws_bytes;
+    D2IC_REQUIRE(need <= (size_t)D2IC_NOALLOC_SCRATCH_BYTES,
+                 "d2ic_cg_solve_noalloc: frame needs %zu bytes of scratch (%d nodes, %d chunks), more than the "
+                 "fixed %zu-byte array; use d2ic_cg_solve_batched with caller-allocated scratch",
+                 need, frame->n_nodes, frame->n_chunks, (size_t)D2IC_NOALLOC_SCRATCH_BYTES);
+    if (g_noalloc_addr[dev] == nullptr) {      // set-up, once per device, with that device current
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(noalloc scratch)");
+        g_noalloc_addr[dev] = p;
+    }
+    char *base = (char *)g_noalloc_addr[dev];
+    d2ic_frame_t f = *frame;                   // caller's inputs/outputs, workspace from the array
+    int st = d2ic_frame_bind_workspace(&f, base + desc_bytes + ctl_bytes);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    // pageable-source copy: returns once `f` has been staged, so the stack copy may go out of scope
+    e = cudaMemcpyAsync(base, &f, sizeof(f), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_status(e, "noalloc descriptor copy");
+    // the launch clears the control header on `s`; the kernel initialises every workspace word it reads
+    return launch_engine((const d2ic_frame_t *)base, 1, base + desc_bytes, ctl_bytes, interp_kind, 0, 0, nullptr,
+                         nullptr, nullptr, nullptr, 0, s);
+}

@@ -154,6 +154,21 @@ D2IC_API int d2ic_cg_solve_traced(const d2ic_frame_t *frames, int n_frames, void
                                   int interp_kind, int grid_blocks, unsigned long long *trace, int trace_rounds,
                                   void *stream);
 
+/* Solve one frame without allocating any device memory: for callers that
+ * cannot call cudaMalloc (a host runtime without a device allocator, a plugin
+ * whose host owns all device memory).  `frame` is a HOST pointer; its inputs
+ * and outputs are used as given and its workspace fields are ignored: the
+ * descriptor copy, control block and CG workspace come from one fixed
+ * file-scope device array of D2IC_NOALLOC_SCRATCH_BYTES, which every GPU that
+ * loads the library holds until the process exits.  A frame needing more
+ * (about 56 B per node + 40 B per chunk + 2 KB) is rejected with D2IC_BAD_ARG.
+ * The first call on a device looks up the array's device address (set-up), so
+ * make it before any stream capture.  All calls share the one array and the
+ * last call's contents stay in it: calls whose work overlaps on the GPU race.
+ * No counterpart in the reference. */
+#define D2IC_NOALLOC_SCRATCH_BYTES (32u << 20)
+D2IC_API int d2ic_cg_solve_noalloc(const d2ic_frame_t *frame, int interp_kind, void *stream);
+
 /* Objective and gradient at u for one frame (the value_and_grad of J_total,
  * d2ic/solver_global_cg.py:323).  frame: device pointer; control: as above for
  * one frame.  Writes J (1 double) and grad (2*n_nodes floats). */
