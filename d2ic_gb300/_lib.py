@@ -46,9 +46,9 @@ class Frame(ctypes.Structure):
     """Mirror of ``d2ic_frame_t``."""
     _fields_ = [
         ("coeff", vp), ("pix", vp), ("chunk_begin", vp), ("chunk_nodes", vp),
-        ("chunk_box", vp), ("node_chunk_ent", vp), ("nbr_index", vp), ("nbr_weight", vp),
+        ("chunk_box", vp), ("chunk_slot", vp), ("nbr_index", vp), ("nbr_weight", vp),
         ("u0", vp), ("u_out", vp), ("hist", vp), ("n_iters", vp), ("status", vp), ("n_evals", vp),
-        ("node_ws", vp), ("chunk_J", vp), ("chunk_grad", vp), ("group_part", vp),
+        ("node_ws", vp), ("chunk_J", vp), ("node_grad", vp), ("group_part", vp),
         ("tol", f64), ("alpha_reg", f32), ("max_iter", i32),
         ("W", i32), ("H", i32), ("cpitch", i32), ("pad", i32),
         ("n_pix", i32), ("n_chunks", i32), ("n_nodes", i32), ("max_deg", i32),
@@ -65,7 +65,7 @@ _SIGS = {
     "d2ic_pad_image": (i32, [vp, i32, i32, i32, i32, vp, vp]),
     "d2ic_sample_points": (i32, [vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, vp, vp]),
     "d2ic_pack_pixels": (i32, [vp, vp, i32, vp, i32, i32, i32, i32, i32, vp, vp]),
-    "d2ic_frame_workspace_bytes": (szt, [i32, i32]),
+    "d2ic_frame_workspace_bytes": (szt, [i32, i32, i32]),
     "d2ic_frame_bind_workspace": (i32, [vp, vp]),
     "d2ic_cg_control_bytes": (szt, [i32]),
     "d2ic_cg_solve_batched": (i32, [vp, i32, vp, szt, i32, i32, vp]),

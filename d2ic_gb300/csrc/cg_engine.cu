@@ -263,8 +263,10 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
         rec[i] = (p < pe) ? __ldg(pix + p) : make_uint4(0u, 0u, 0u, 0u);
     }
     float2 uc = make_float2(0.f, 0.f);
+    int nd = 0, slot = 0;
     if (lane < 4) {
-        const int nd = __ldg(F.chunk_nodes + 4 * c + lane);
+        nd = __ldg(F.chunk_nodes + 4 * c + lane);
+        slot = (int)(((unsigned)__ldg(F.chunk_slot + c) >> (8 * lane)) & 0xffu);
         float2 dir;
         uc = cd.at(nd, dir);
     }
@@ -334,17 +336,17 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
     for (int i = 0; i < RPL; ++i)
         if (pb + lane + 32 * i < pe) one(rec[i]);
     for (int p = pb + lane + 32 * RPL; p < pe; p += 32) one(__ldg(pix + p));   // chunks longer than the prefetch
-    const double js = warp_sum_d((double)jr);
+    const DF js = df_warp_sum(DF{jr, 0.f});
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         gxa[a] = warp_sum_f(gxa[a]);
         gya[a] = warp_sum_f(gya[a]);
     }
-    if (lane == 0) {
-        F.chunk_J[c] = js;
-        float4 *cg = reinterpret_cast<float4 *>(F.chunk_grad + 8 * (size_t)c);
-        cg[0] = make_float4(gxa[0], gxa[1], gxa[2], gxa[3]);
-        cg[1] = make_float4(gya[0], gya[1], gya[2], gya[3]);
+    if (lane == 0) reinterpret_cast<float2 *>(F.chunk_J)[c] = make_float2(js.hi, js.lo);   // double-float
+    if (lane < 4) {                                 // lane a stores node a's partial in the chunk's slot
+        const float gx = lane == 0 ? gxa[0] : lane == 1 ? gxa[1] : lane == 2 ? gxa[2] : gxa[3];
+        const float gy = lane == 0 ? gya[0] : lane == 1 ? gya[1] : lane == 2 ? gya[2] : gya[3];
+        reinterpret_cast<float2 *>(F.node_grad)[(size_t)slot * F.n_nodes + nd] = make_float2(gx, gy);
     }
     __syncwarp();                                   // the tile is reused by the warp's next chunk
 }
@@ -352,11 +354,11 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
 // ---------------------------------------------------------------------------
 // N phase: one group of NG nodes per block
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameState *S, int g, double (*red)[NWARP]) {
+__device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameState *S, int g, DF (*red)[NWARP]) {
     const Cand cd = make_cand(F, S);
     const int n = g * NG + threadIdx.x;
     const int igt = __ldcg(&S->igt), igc = __ldcg(&S->igc), iu = __ldcg(&S->iu), idp = __ldcg(&S->idp);
-    double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    DF q[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     if (n < F.n_nodes) {
         // All loads of a batch are issued before any is consumed: the node pass
         // is a short chain of L2 round trips instead of one per table entry.
@@ -365,27 +367,19 @@ __device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameSta
         const float2 gc = __ldcg(nbuf(F, 2 + igc) + n);  // issued with the candidate's own loads
         float2 dir;
         const float2 ui = cd.at(n, dir);
+        // chunk partials from the node's K slots (unused slots hold 0), in slot order
         float sx = 0.f, sy = 0.f;
         const int K = F.node_chunk_k, Nn = F.n_nodes;
-        for (int eb = 0; eb < K; eb += NB) {
-            int ent[NB];
+        const float2 *ng = reinterpret_cast<const float2 *>(F.node_grad) + n;
+        for (int kb = 0; kb < K; kb += NB) {
+            float2 v[NB];
 #pragma unroll
-            for (int q = 0; q < NB; ++q) ent[q] = (eb + q < K) ? __ldg(F.node_chunk_ent + (size_t)(eb + q) * Nn + n) : -1;
-            float vx[NB], vy[NB];
-#pragma unroll
-            for (int q = 0; q < NB; ++q) {
-                vx[q] = vy[q] = 0.f;
-                if (ent[q] >= 0) {
-                    const float *cgp = F.chunk_grad + 8 * (size_t)(ent[q] >> 2) + (ent[q] & 3);
-                    vx[q] = __ldcg(cgp);
-                    vy[q] = __ldcg(cgp + 4);
-                }
-            }
+            for (int q = 0; q < NB; ++q) v[q] = (kb + q < K) ? __ldcg(ng + (size_t)(kb + q) * Nn) : make_float2(0.f, 0.f);
 #pragma unroll
             for (int q = 0; q < NB; ++q)
-                if (ent[q] >= 0) {
-                    sx += vx[q];
-                    sy += vy[q];
+                if (kb + q < K) {
+                    sx += v[q].x;
+                    sy += v[q].y;
                 }
         }
         float rx = 0.f, ry = 0.f, en = 0.f;
@@ -425,28 +419,36 @@ __device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameSta
         nbuf(F, 2 + igt)[n] = make_float2(gx, gy);
         nbuf(F, 1 - iu)[n] = ui;
         nbuf(F, 5 + (1 - idp))[n] = dir;
-        q[P_EREG] = 0.25 * (double)en;
-        q[P_GG] = (double)gx * gx + (double)gy * gy;
-        q[P_GDIFF] = (double)gx * ((double)gx - gc.x) + (double)gy * ((double)gy - gc.y);
-        q[P_GD] = (double)gc.x * dir.x + (double)gc.y * dir.y;
+        // per-node terms of the inner products, exact in double-float (g - g_cur rounded
+        // in FP32 as the reference's elementwise difference)
+        q[P_EREG] = DF{0.25f * en, 0.f};
+        q[P_GG] = df_add(df_prod(gx, gx), df_prod(gy, gy));
+        q[P_GDIFF] = df_add(df_prod(gx, gx - gc.x), df_prod(gy, gy - gc.y));
+        q[P_GD] = df_add(df_prod(gc.x, dir.x), df_prod(gc.y, dir.y));
     }
     // this group's share of the chunk sums of r^2
     {
         const int c0 = g * F.chunks_per_group;
         const int c1 = min(c0 + F.chunks_per_group, F.n_chunks);
-        for (int c = c0 + (int)threadIdx.x; c < c1; c += NG) q[P_JSUM] += __ldcg(F.chunk_J + c);
+        const float2 *cj = reinterpret_cast<const float2 *>(F.chunk_J);
+        for (int c = c0 + (int)threadIdx.x; c < c1; c += NG) {
+            const float2 v = __ldcg(cj + c);
+            q[P_JSUM] = df_add(q[P_JSUM], DF{v.x, v.y});
+        }
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-        const double v = warp_sum_d(q[i]);
+        const DF v = df_warp_sum(q[i]);
         if (lane == 0) red[i][wid] = v;
     }
     __syncthreads();
-    if (threadIdx.x < 5) {
-        double s = 0.0;
-        for (int w = 0; w < NWARP; ++w) s += red[threadIdx.x][w];
-        F.group_part[(size_t)g * D2IC_NPART + threadIdx.x] = s;
+    if (wid == 0) {                                // warp 0: one warp-sum per quantity, fixed order
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+            const DF v = df_warp_sum(lane < NWARP ? red[i][lane] : DF{0.f, 0.f});
+            if (lane == 0) F.group_part[(size_t)g * D2IC_NPART + i] = df_to_double(v);
+        }
     }
     __syncthreads();
 }
@@ -499,6 +501,11 @@ __device__ void frame_decide(FrameState &S, const d2ic_frame_t &F, const double 
     const double J = 0.5 * q[P_JSUM] / (double)max(F.n_pix, 1) + (double)F.alpha_reg * q[P_EREG];
     if (J != J || q[P_GG] != q[P_GG]) S.nan_seen = 1;
     S.n_evals += 1;
+    // control-flow guard: an iteration takes at most 11 evaluations plus one restart
+    if (S.n_evals > 12 * max(F.max_iter, 0) + 4) {
+        S.state = ST_DONE;
+        return;
+    }
     switch (S.state) {
         case ST_EVAL:
             accept_point(S, J, q[P_GG], q[P_GDIFF]);
@@ -601,15 +608,6 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
             gp += frames[f].n_groups;
         }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        C.h->work = 0;
-        C.h->rounds += 1;
-        if (C.h->rounds > C.h->max_rounds) {        // control-flow guard: never spin forever
-            C.h->err = D2IC_MAX_ITERS;
-            C.h->abort = 1;
-        }
-        __threadfence();
-    }
 }
 
 __device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
@@ -663,15 +661,7 @@ __device__ void r_step(const d2ic_frame_t *frames, int n_frames, Ctl &C, int eva
         }
     }
     __syncthreads();
-    if (s_finished) {
-        rebuild_active(frames, n_frames, C);
-    } else if (threadIdx.x == 0) {                     // active set unchanged: keep the lists
-        C.h->rounds += 1;
-        if (C.h->rounds > C.h->max_rounds) {
-            C.h->err = D2IC_MAX_ITERS;
-            C.h->abort = 1;
-        }
-    }
+    if (s_finished) rebuild_active(frames, n_frames, C);   // else the active lists stay as they are
 }
 
 // ---------------------------------------------------------------------------
@@ -682,7 +672,7 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                                                    char *ctl_base, int eval_only, const float *u_eval,
                                                    double *J_out, float *grad_out, unsigned long long *trace,
                                                    int trace_rounds) {
-    __shared__ double red[5][NWARP];
+    __shared__ DF red[5][NWARP];
     extern __shared__ float s_tile[];              // NWARP * TILE_CAP floats
     Ctl C = make_ctl(ctl_base, n_frames);
     const int lane = threadIdx.x & 31;
@@ -702,6 +692,10 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
 #pragma unroll
             for (int j = 1; j < 7; ++j) nbuf(F, j)[i] = make_float2(0.f, 0.f);
         }
+        // gradient slots that no chunk owns must read as 0
+        float2 *ng = reinterpret_cast<float2 *>(F.node_grad);
+        for (size_t i = blockIdx.x * NG + threadIdx.x; i < (size_t)F.node_chunk_k * nn; i += (size_t)gridDim.x * NG)
+            ng[i] = make_float2(0.f, 0.f);
         if (F.hist)
             for (int i = blockIdx.x * NG + threadIdx.x; i < 3 * F.max_iter; i += gridDim.x * NG)
                 F.hist[i] = __int_as_float(0x7fc00000);
@@ -864,11 +858,12 @@ extern "C" size_t d2ic_cg_control_bytes(int n_frames) {
     return ctl_layout(n_frames, &a, &b, &c, &d);
 }
 
-extern "C" size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks) {
+extern "C" size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks, int node_chunk_k) {
     const int ng = (n_nodes + NG - 1) / NG;
+    if (node_chunk_k < 1) node_chunk_k = 1;
     size_t off = align256(sizeof(float) * 14 * (size_t)n_nodes);
     off += align256(sizeof(double) * (size_t)n_chunks);
-    off += align256(sizeof(float) * 8 * (size_t)n_chunks);
+    off += align256(sizeof(float) * 2 * (size_t)node_chunk_k * n_nodes);
     off += align256(sizeof(double) * D2IC_NPART * (size_t)(ng > 0 ? ng : 1));
     return off;
 }
@@ -876,14 +871,15 @@ extern "C" size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks) {
 extern "C" int d2ic_frame_bind_workspace(d2ic_frame_t *f, void *ws) {
     D2IC_REQUIRE(f && ws, "d2ic_frame_bind_workspace: null pointer");
     D2IC_REQUIRE(((uintptr_t)ws & 255) == 0, "d2ic_frame_bind_workspace: workspace must be 256-byte aligned");
-    D2IC_REQUIRE(f->n_nodes >= 1 && f->n_chunks >= 0, "d2ic_frame_bind_workspace: bad sizes");
+    D2IC_REQUIRE(f->n_nodes >= 1 && f->n_chunks >= 0 && f->node_chunk_k >= 1 && f->node_chunk_k <= 255,
+                 "d2ic_frame_bind_workspace: bad sizes");
     char *p = (char *)ws;
     f->node_ws = (float *)p;
     p += align256(sizeof(float) * 14 * (size_t)f->n_nodes);
     f->chunk_J = (double *)p;
     p += align256(sizeof(double) * (size_t)f->n_chunks);
-    f->chunk_grad = (float *)p;
-    p += align256(sizeof(float) * 8 * (size_t)f->n_chunks);
+    f->node_grad = (float *)p;
+    p += align256(sizeof(float) * 2 * (size_t)f->node_chunk_k * f->n_nodes);
     f->group_part = (double *)p;
     f->n_groups = (f->n_nodes + NG - 1) / NG;
     f->chunks_per_group = (f->n_chunks + f->n_groups - 1) / f->n_groups;
@@ -941,7 +937,8 @@ extern "C" int d2ic_cg_solve_noalloc(const d2ic_frame_t *frame, int interp_kind,
     D2IC_REQUIRE(dev >= 0 && dev < 64, "d2ic_cg_solve_noalloc: device index %d out of range", dev);
     const size_t desc_bytes = align256(sizeof(d2ic_frame_t));
     const size_t ctl_bytes = d2ic_cg_control_bytes(1);
-    const size_t ws_bytes = d2ic_frame_workspace_bytes(frame->n_nodes, frame->n_chunks);
+    D2IC_REQUIRE(frame->node_chunk_k >= 1 && frame->node_chunk_k <= 255, "d2ic_cg_solve_noalloc: bad node_chunk_k");
+    const size_t ws_bytes = d2ic_frame_workspace_bytes(frame->n_nodes, frame->n_chunks, frame->node_chunk_k);
     const size_t need = desc_bytes + ctl_bytes + ws_bytes;
     D2IC_REQUIRE(need <= (size_t)D2IC_NOALLOC_SCRATCH_BYTES,
                  "d2ic_cg_solve_noalloc: frame needs %zu bytes of scratch (%d nodes, %d chunks), more than the "

@@ -147,6 +147,41 @@ __device__ __forceinline__ void split_coord(int i, float d, int &ib, float &t) {
     t = d - fl;
 }
 
+// Double-float ("hi + lo") accumulation: TwoSum / TwoProduct are error-free
+// transformations in FP32 (Knuth; Ogita, Rump & Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 2005), giving ~48-bit sums at FP32 issue
+// rate.  GB300's FP64 pipe runs at a small fraction of FP32, so the inner
+// products of the CG control are accumulated this way and converted to FP64
+// once per group.  df_add is commutative bit for bit, so xor-butterfly warp
+// reductions leave every lane with the same value.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+    const DF s = df_two_sum(x.hi, y.hi);
+    const float e = s.lo + (x.lo + y.lo);
+    const float h = s.hi + e;
+    return {h, e - (h - s.hi)};
+}
+__device__ __forceinline__ DF df_prod(float a, float b) {
+    const float p = a * b;
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ DF df_warp_sum(DF v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const DF w = {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+        v = df_add(v, w);
+    }
+    return v;
+}
+__device__ __forceinline__ double df_to_double(DF v) { return (double)v.hi + (double)v.lo; }
+
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

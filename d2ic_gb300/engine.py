@@ -11,8 +11,10 @@ Data layout in HBM (per reference image + mesh, built once by
   nodes of the chunk's element;
 * ``chunk_box`` (Nc, 2): inclusive pixel box of each chunk, which bounds the
   chunk's shared-memory coefficient tile;
-* ``node_chunk_ent`` (K, Nn): node -> (chunk, local slot) table, the transpose
-  of the chunk -> node gather (no atomics), column-major, -1 padded;
+* ``chunk_slot`` (Nc,): for each of the chunk's 4 nodes, the slot (rank of the
+  chunk among the node's chunks) where the pixel pass stores the chunk's
+  gradient partial for that node; the node pass sums its K slots in order --
+  the transpose of the chunk -> node gather without atomics;
 * ``nbr_index`` / ``nbr_weight`` (max_deg, Nn): the spring table, column-major,
   weights pre-multiplied by (rho_i + rho_j)/2 in FP32.
 
@@ -157,15 +159,18 @@ class FrameLayout:
             chunk_box = chunk_box.astype(np.uint32).view(np.int32)
         else:
             chunk_box = np.zeros((0, 2), np.int32)
-        # node -> (chunk << 2 | slot) table, fixed width K, column-major, ascending chunk order
+        # node gradient slots: the chunk's partial for its local node a goes to slot rank(chunk) of
+        # that node, ranks in ascending chunk order; K = most chunks meeting at one node
         flat = chunk_nodes.reshape(-1).astype(np.int64)
-        ent = (np.repeat(np.arange(self.n_chunks, dtype=np.int64), 4) << 2) | np.tile(np.arange(4), self.n_chunks)
         o = np.argsort(flat, kind="stable")
         cnt = np.bincount(flat, minlength=self.n_nodes)
         K = max(int(cnt.max(initial=0)), 1)
-        rank = np.arange(flat.size) - np.repeat(np.cumsum(cnt) - cnt, cnt)
-        node_chunk_ent = -np.ones((K, self.n_nodes), dtype=np.int32)
-        node_chunk_ent[rank, flat[o]] = ent[o]
+        if K > 255:
+            raise ValueError(f"a node touches {K} chunks; at most 255 are supported")
+        rank = np.empty(flat.size, dtype=np.int64)
+        rank[o] = np.arange(flat.size) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+        r4 = rank.reshape(-1, 4)
+        chunk_slot = (r4[:, 0] | (r4[:, 1] << 8) | (r4[:, 2] << 16) | (r4[:, 3] << 24)).astype(np.uint32).view(np.int32)
         self.node_chunk_k = K
         # spring table: entries beyond the degree are padding; column-major for coalesced node-pass loads
         nbi = np.asarray(pix.node_neighbor_index, dtype=np.int64).reshape(self.n_nodes, -1)
@@ -187,7 +192,7 @@ class FrameLayout:
         self.chunk_begin = T(chunk_begin)
         self.chunk_nodes = T(chunk_nodes)
         self.chunk_box = T(chunk_box) if self.n_chunks else torch.zeros((1, 2), dtype=torch.int32, device=dev)
-        self.node_chunk_ent = T(node_chunk_ent)
+        self.chunk_slot = T(chunk_slot) if self.n_chunks else torch.zeros((1,), dtype=torch.int32, device=dev)
         self.nbr_index = T(nbr_index) if md else torch.full((1,), -1, dtype=torch.int32, device=dev)
         self.nbr_weight = T(nbr_weight) if md else torch.zeros((1,), dtype=torch.float32, device=dev)
         self.pixel_order = order
@@ -219,7 +224,7 @@ class FrameSlot:
         self.u_out = torch.zeros((L.n_nodes, 2), dtype=torch.float32, device=dev)
         self.hist = torch.full((max(self.max_iter, 1), 3), float("nan"), dtype=torch.float32, device=dev)
         self.info = torch.zeros(3, dtype=torch.int32, device=dev)          # n_iters, status, n_evals
-        nb = _lib.load().d2ic_frame_workspace_bytes(L.n_nodes, L.n_chunks)
+        nb = _lib.load().d2ic_frame_workspace_bytes(L.n_nodes, L.n_chunks, L.node_chunk_k)
         self.ws = torch.empty(nb, dtype=torch.uint8, device=dev)
         self.desc = self._descriptor(1e-6, 0.0)
 
@@ -231,7 +236,7 @@ class FrameSlot:
         f.chunk_begin = ptr(L.chunk_begin)
         f.chunk_nodes = ptr(L.chunk_nodes)
         f.chunk_box = ptr(L.chunk_box)
-        f.node_chunk_ent = ptr(L.node_chunk_ent)
+        f.chunk_slot = ptr(L.chunk_slot)
         f.node_chunk_k = L.node_chunk_k
         f.nbr_index = ptr(L.nbr_index)
         f.nbr_weight = ptr(L.nbr_weight)

@@ -70,9 +70,9 @@ typedef struct d2ic_frame {
     const int   *chunk_nodes;      /* 4 * n_chunks, the chunk's element nodes (Q4 order) */
     const int   *chunk_box;        /* 2 * n_chunks: (col0 | row0 << 16, col1 | row1 << 16),
                                       inclusive pixel box of the chunk                  */
-    const int   *node_chunk_ent;   /* node_chunk_k * n_nodes, column-major (slot k of node
-                                      n at k * n_nodes + n): (chunk << 2) | local node
-                                      slot, in ascending chunk order, -1 padded           */
+    const int   *chunk_slot;       /* n_chunks: byte a = rank of the chunk among the chunks
+                                      of its local node a (ascending chunk order), i.e.
+                                      the node_grad slot the chunk's partial goes to     */
     const int   *nbr_index;        /* max_deg * n_nodes spring neighbours, column-major,
                                       -1 padded after the last neighbour                */
     const float *nbr_weight;       /* same layout: w_ij * (rho_i + rho_j) / 2           */
@@ -84,8 +84,11 @@ typedef struct d2ic_frame {
     int         *n_evals;          /* 1: objective evaluations (pixel passes) performed */
     /* workspace */
     float       *node_ws;          /* 14 * n_nodes floats                               */
-    double      *chunk_J;          /* n_chunks                                          */
-    float       *chunk_grad;       /* 8 * n_chunks                                      */
+    double      *chunk_J;          /* n_chunks x 8 bytes: each chunk's sum of r^2 as a
+                                      double-float (hi, lo) pair                         */
+    float       *node_grad;        /* 2 * node_chunk_k * n_nodes: per-node slots of the
+                                      chunks' gradient partials, column-major (slot k of
+                                      node n at k * n_nodes + n), unused slots stay 0    */
     double      *group_part;       /* D2IC_NPART * n_groups                             */
     double       tol;
     float        alpha_reg;
@@ -131,7 +134,7 @@ D2IC_API int d2ic_pack_pixels(const int *colrow, const float *xieta, int n,
 
 /* Bytes of per-frame workspace, and binding of a workspace block to a frame
  * descriptor (host-side; `ws` is a device pointer aligned to 256 bytes). */
-D2IC_API size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks);
+D2IC_API size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks, int node_chunk_k);
 D2IC_API int d2ic_frame_bind_workspace(d2ic_frame_t *frame, void *ws);
 
 /* Bytes of launch-wide control scratch for a batched launch of n_frames. */
@@ -161,7 +164,8 @@ D2IC_API int d2ic_cg_solve_traced(const d2ic_frame_t *frames, int n_frames, void
  * descriptor copy, control block and CG workspace come from one fixed
  * file-scope device array of D2IC_NOALLOC_SCRATCH_BYTES, which every GPU that
  * loads the library holds until the process exits.  A frame needing more
- * (about 56 B per node + 40 B per chunk + 2 KB) is rejected with D2IC_BAD_ARG.
+ * (about (56 + 8 node_chunk_k) B per node + 8 B per chunk + 2 KB) is rejected
+ * with D2IC_BAD_ARG.
  * The first call on a device looks up the array's device address (set-up), so
  * make it before any stream capture.  All calls share the one array and the
  * last call's contents stay in it: calls whose work overlaps on the GPU race.

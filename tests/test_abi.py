@@ -20,13 +20,13 @@ def test_host_only_entry_points(built_library):
     assert built_library.d2ic_version() >= 100
     assert built_library.d2ic_cg_control_bytes(1) > 0
     assert built_library.d2ic_cg_control_bytes(64) > built_library.d2ic_cg_control_bytes(1)
-    nb = built_library.d2ic_frame_workspace_bytes(1089, 784)
-    assert nb >= 14 * 4 * 1089 + 784 * (8 + 32)
+    nb = built_library.d2ic_frame_workspace_bytes(1089, 784, 4)
+    assert nb >= 14 * 4 * 1089 + 784 * 8 + 4 * 8 * 1089
     f = _lib.Frame()
-    f.n_nodes, f.n_chunks = 1089, 784
+    f.n_nodes, f.n_chunks, f.node_chunk_k = 1089, 784, 4
     fake_ws = 1 << 20                      # never dereferenced: binding only computes addresses
     assert built_library.d2ic_frame_bind_workspace(ctypes.byref(f), fake_ws) == 0
     assert f.node_ws == fake_ws and f.n_groups == 3 and f.chunks_per_group == 262
-    assert f.chunk_J % 256 == 0 and f.chunk_grad % 256 == 0 and f.group_part % 256 == 0
+    assert f.chunk_J % 256 == 0 and f.node_grad % 256 == 0 and f.group_part % 256 == 0
     assert built_library.d2ic_frame_bind_workspace(ctypes.byref(f), fake_ws + 8) == _lib.BAD_ARG
     assert b"256-byte" in built_library.d2ic_last_error_string()

@@ -74,6 +74,7 @@ def test_noalloc_rejects_oversize_frame(cuda):
     f = _lib.Frame()
     f.n_nodes = 4_000_000          # far beyond the fixed scratch array
     f.n_chunks = 1
+    f.node_chunk_k = 4
     L = _lib.load()
     assert L.d2ic_cg_solve_noalloc(ctypes.byref(f), _lib.INTERP_CUBIC, _lib.stream_handle()) == _lib.BAD_ARG
     assert b"fixed" in L.d2ic_last_error_string()
