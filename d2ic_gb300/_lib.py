@@ -23,6 +23,8 @@ MAX_ITERS = -4
 WAIT_TIMEOUT = -5
 CUDA_ERROR = -6
 UNSUPPORTED = -7
+RUNNING = 1
+CMD_INIT, CMD_RUN, CMD_IDLE = 0, 1, 2
 
 INTERP_CUBIC = 0
 INTERP_LINEAR = 1
@@ -33,7 +35,7 @@ CHUNK_MAX = 256
 
 STATUS_NAMES = {OK: "ok", BAD_ARG: "bad_arg", OOM: "oom", NAN_DETECTED: "nan_detected",
                 MAX_ITERS: "max_iters", WAIT_TIMEOUT: "wait_timeout", CUDA_ERROR: "cuda_error",
-                UNSUPPORTED: "unsupported"}
+                UNSUPPORTED: "unsupported", RUNNING: "running"}
 
 vp = ctypes.c_void_p
 i32 = ctypes.c_int
@@ -71,6 +73,8 @@ _SIGS = {
     "d2ic_cg_solve_batched": (i32, [vp, i32, vp, szt, i32, i32, vp]),
     "d2ic_cg_solve_traced": (i32, [vp, i32, vp, szt, i32, i32, vp, i32, vp]),
     "d2ic_cg_solve_noalloc": (i32, [vp, i32, vp]),
+    "d2ic_cg_command_offset": (szt, []),
+    "d2ic_cg_slice": (i32, [vp, i32, vp, szt, i32, i32, i32, vp]),
     "d2ic_eval_objective": (i32, [vp, vp, vp, szt, i32, vp, vp, vp]),
     "d2ic_zncc_match": (i32, [vp, i32, i32, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp]),
     "d2ic_idw_project": (i32, [vp, i32, vp, vp, i32, f32, vp, vp]),

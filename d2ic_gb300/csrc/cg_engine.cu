@@ -64,7 +64,12 @@ struct FrameState {
     int state, k, t, restart, gd_known, nan_seen;
     int iu, igp, igc, igt, idp;
     int n_evals;
+    int reported;   // outputs of a finished frame were written by an earlier launch
+    int pad2_;
 };
+
+// per-frame commands written by the host between launches (control block, after the header)
+enum { CMD_INIT = 0, CMD_RUN = 1, CMD_IDLE = 2 };
 
 struct CtlHeader {
     unsigned bar_count;
@@ -82,6 +87,7 @@ struct CtlHeader {
 
 struct Ctl {
     CtlHeader *h;
+    int *cmd;      // n_frames: CMD_INIT / CMD_RUN / CMD_IDLE
     int *active;   // n_frames
     int *cpre;     // n_frames + 1
     int *gpre;     // n_frames + 1
@@ -90,8 +96,10 @@ struct Ctl {
 
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// control block: header | cmd | active | cpre | gpre | frame states
 __host__ __device__ inline size_t ctl_layout(int n, size_t *o_active, size_t *o_cpre, size_t *o_gpre, size_t *o_fs) {
     size_t off = align256(sizeof(CtlHeader));
+    off = align256(off + sizeof(int) * (size_t)n);          // cmd
     *o_active = off;
     off = align256(off + sizeof(int) * (size_t)n);
     *o_cpre = off;
@@ -108,6 +116,7 @@ __device__ inline Ctl make_ctl(char *base, int n) {
     ctl_layout(n, &oa, &oc, &og, &of);
     Ctl c;
     c.h = (CtlHeader *)base;
+    c.cmd = (int *)(base + align256(sizeof(CtlHeader)));
     c.active = (int *)(base + oa);
     c.cpre = (int *)(base + oc);
     c.gpre = (int *)(base + og);
@@ -610,27 +619,31 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
     __syncthreads();
 }
 
+// Start of a launch: new frames (CMD_INIT) get a fresh CG state, idle slots are
+// parked as finished-and-reported, running frames keep their state; frames
+// that finished in an earlier launch are marked reported (their outputs were
+// written at the end of that launch).
 __device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
-    int mr = 0;
     for (int f = threadIdx.x; f < n_frames; f += NG) {
-        FrameState S;
-        S.J_cur = S.gg_cur = S.gg_prev = S.gdiff_cur = S.gd = S.J_last = S.gnorm = 0.0;
-        S.alpha = 0.f;
-        S.beta = 0.f;
-        S.k = S.t = S.restart = S.gd_known = S.nan_seen = S.n_evals = 0;
-        S.iu = 0; S.igp = 0; S.igc = 1; S.igt = 2; S.idp = 0;
-        S.state = ST_EVAL;
-        C.fs[f] = S;
-        mr = max(mr, 12 * max(frames[f].max_iter, 0) + 4);
-    }
-    __shared__ int s_mr[NG];
-    s_mr[threadIdx.x] = mr;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int m = 0;
-        for (int i = 0; i < NG; ++i) m = max(m, s_mr[i]);
-        C.h->max_rounds = m;
-        C.h->rounds = 0;
+        const int cmd = ld_vol(C.cmd + f);
+        if (cmd == CMD_INIT) {
+            FrameState S;
+            S.J_cur = S.gg_cur = S.gg_prev = S.gdiff_cur = S.gd = S.J_last = S.gnorm = 0.0;
+            S.alpha = 0.f;
+            S.beta = 0.f;
+            S.k = S.t = S.restart = S.gd_known = S.nan_seen = S.n_evals = 0;
+            S.iu = 0; S.igp = 0; S.igc = 1; S.igt = 2; S.idp = 0;
+            S.state = ST_EVAL;
+            S.reported = 0;
+            S.pad2_ = 0;
+            C.fs[f] = S;
+            C.cmd[f] = CMD_RUN;
+        } else if (cmd == CMD_IDLE) {
+            C.fs[f].state = ST_DONE;
+            C.fs[f].reported = 1;
+        } else if (ld_vol(&C.fs[f].state) == ST_DONE) {
+            C.fs[f].reported = 1;
+        }
     }
     __syncthreads();
     rebuild_active(frames, n_frames, C);
@@ -671,7 +684,7 @@ template <int KIND>
 __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
                                                    char *ctl_base, int eval_only, const float *u_eval,
                                                    double *J_out, float *grad_out, unsigned long long *trace,
-                                                   int trace_rounds) {
+                                                   int trace_rounds, int max_rounds) {
     __shared__ DF red[5][NWARP];
     extern __shared__ float s_tile[];              // NWARP * TILE_CAP floats
     Ctl C = make_ctl(ctl_base, n_frames);
@@ -682,8 +695,9 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     const bool tr = trace != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
     int round = 0;
 
-    // ---- init: u <- u0, zero g/d buffers, NaN history ----
+    // ---- init of newly admitted frames: u <- u0, zero g/d buffers and gradient slots, NaN history ----
     for (int f = 0; f < n_frames; ++f) {
+        if (ld_vol(C.cmd + f) != CMD_INIT) continue;
         const d2ic_frame_t &F = frames[f];
         const int nn = F.n_nodes;
         const float2 *u0 = reinterpret_cast<const float2 *>((eval_only && u_eval && f == 0) ? u_eval : F.u0);
@@ -702,7 +716,7 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     }
     if (!grid_barrier(C.h, [&] { r_init(frames, n_frames, C); })) goto finish;
 
-    while (true) {
+    while (round < max_rounds) {                    // a slice: at most max_rounds rounds, state kept in HBM
         const int na = ld_vol(&C.h->n_active);
         if (na == 0) break;
         const bool trr = tr && round < trace_rounds;
@@ -755,10 +769,16 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     }
 
 finish:
-    // ---- outputs ----
+    // ---- outputs of frames that finished in this launch; running frames report D2IC_RUNNING ----
+    const bool aborted = ld_vol(&C.h->abort) != 0;
     for (int f = 0; f < n_frames; ++f) {
         const d2ic_frame_t &F = frames[f];
         const FrameState *S = C.fs + f;
+        const bool done = ld_vol(&S->state) == ST_DONE;
+        if (!(aborted || eval_only || (done && !ld_vol(&S->reported)))) {
+            if (!done && blockIdx.x == 0 && threadIdx.x == 0 && F.status) *F.status = D2IC_RUNNING;
+            continue;
+        }
         const int iu = ld_vol(&S->iu), igc = ld_vol(&S->igc);
         const int nn = F.n_nodes;
         float2 *uo = reinterpret_cast<float2 *>(F.u_out);
@@ -770,7 +790,7 @@ finish:
             if (F.n_iters) *F.n_iters = ld_vol(&S->k);
             if (F.n_evals) *F.n_evals = ld_vol(&S->n_evals);
             int st = D2IC_OK;
-            if (ld_vol(&C.h->abort)) st = ld_vol(&C.h->err);
+            if (aborted) st = ld_vol(&C.h->err);
             else if (ld_vol(&S->nan_seen)) st = D2IC_NAN_DETECTED;
             else if (ld_vol(&S->k) >= F.max_iter && F.max_iter > 0) st = D2IC_MAX_ITERS;
             if (F.status) *F.status = st;
@@ -816,7 +836,8 @@ static int dev_info(int dev, DevInfo **out) {
 
 static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes, int kind,
                          int grid_blocks, int eval_only, const float *u_eval, double *J_out, float *grad_out,
-                         unsigned long long *trace, int trace_rounds, cudaStream_t s) {
+                         unsigned long long *trace, int trace_rounds, cudaStream_t s, int max_rounds = 0x7fffffff,
+                         bool new_batch = true) {
     D2IC_REQUIRE(frames && control, "cg engine: null pointer");
     D2IC_REQUIRE(n_frames >= 1 && n_frames <= D2IC_MAX_FRAMES, "cg engine: n_frames %d out of [1, %d]", n_frames,
                  D2IC_MAX_FRAMES);
@@ -833,18 +854,29 @@ static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control
     const int maxb = di->sms * di->bps[kind == D2IC_INTERP_LINEAR];
     D2IC_REQUIRE(maxb > 0, "cg engine: kernel cannot be resident on this device");
     int blocks = grid_blocks > 0 ? (grid_blocks < maxb ? grid_blocks : maxb) : maxb;
-    e = cudaMemsetAsync(control, 0, sizeof(CtlHeader), s);
+    // header always; with new_batch also the command words (all frames CMD_INIT == 0)
+    const size_t clear = new_batch ? align256(sizeof(CtlHeader)) + sizeof(int) * (size_t)n_frames : sizeof(CtlHeader);
+    e = cudaMemsetAsync(control, 0, clear, s);
     if (e != cudaSuccess) return cuda_status(e, "control reset");
     char *cb = (char *)control;
-    void *args[] = {(void *)&frames, (void *)&n_frames, (void *)&cb, (void *)&eval_only, (void *)&u_eval,
-                    (void *)&J_out, (void *)&grad_out, (void *)&trace, (void *)&trace_rounds};
+    // cooperative launch through cudaLaunchKernelEx (co-residency checked by the driver; capturable)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(NG);
+    cfg.dynamicSmemBytes = ENGINE_SMEM;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     if (kind == D2IC_INTERP_CUBIC)
-        e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_CUBIC>, dim3(blocks), dim3(NG), args,
-                                        ENGINE_SMEM, s);
+        e = cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_CUBIC>, frames, n_frames, cb, eval_only, u_eval, J_out,
+                               grad_out, trace, trace_rounds, max_rounds);
     else
-        e = cudaLaunchCooperativeKernel((const void *)cg_engine<D2IC_INTERP_LINEAR>, dim3(blocks), dim3(NG), args,
-                                        ENGINE_SMEM, s);
-    if (e != cudaSuccess) return cuda_status(e, "cudaLaunchCooperativeKernel(cg_engine)");
+        e = cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_LINEAR>, frames, n_frames, cb, eval_only, u_eval, J_out,
+                               grad_out, trace, trace_rounds, max_rounds);
+    if (e != cudaSuccess) return cuda_status(e, "cooperative launch of cg_engine");
     return D2IC_OK;
 }
 
@@ -899,6 +931,15 @@ extern "C" int d2ic_cg_solve_batched(const d2ic_frame_t *frames, int n_frames, v
                                      int interp_kind, int grid_blocks, void *stream) {
     return launch_engine(frames, n_frames, control, control_bytes, interp_kind, grid_blocks, 0, nullptr, nullptr,
                          nullptr, nullptr, 0, (cudaStream_t)stream);
+}
+
+extern "C" size_t d2ic_cg_command_offset(void) { return align256(sizeof(CtlHeader)); }
+
+extern "C" int d2ic_cg_slice(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
+                             int interp_kind, int grid_blocks, int max_rounds, void *stream) {
+    D2IC_REQUIRE(max_rounds >= 1, "d2ic_cg_slice: max_rounds must be >= 1 (got %d)", max_rounds);
+    return launch_engine(frames, n_frames, control, control_bytes, interp_kind, grid_blocks, 0, nullptr, nullptr,
+                         nullptr, nullptr, 0, (cudaStream_t)stream, max_rounds, false);
 }
 
 extern "C" int d2ic_cg_solve_traced(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,

@@ -294,6 +294,19 @@ class Engine:
         _lib.call("d2ic_cg_solve_batched", ptr(desc_dev), n_frames, ptr(self.control), self.control.numel(), kind,
                   grid_blocks, _lib.stream_handle(stream))
 
+    def commands(self, n_frames: int) -> torch.Tensor:
+        """The per-frame command words inside the control block (int32 view)."""
+        off = _lib.load().d2ic_cg_command_offset()
+        return self.control[off: off + 4 * n_frames].view(torch.int32)
+
+    def run_slice(self, desc_dev: torch.Tensor, n_frames: int, kind: int, max_rounds: int, grid_blocks: int = 0,
+                  stream=None):
+        """Advance every admitted frame by at most ``max_rounds`` objective evaluations."""
+        if n_frames > self.max_frames:
+            raise ValueError(f"{n_frames} frames > engine capacity {self.max_frames}")
+        _lib.call("d2ic_cg_slice", ptr(desc_dev), n_frames, ptr(self.control), self.control.numel(), kind,
+                  grid_blocks, int(max_rounds), _lib.stream_handle(stream))
+
     def solve_traced(self, desc_dev: torch.Tensor, n_frames: int, kind: int, rounds: int = 4096, grid_blocks: int = 0):
         """Solve; per-round durations in microseconds: block 0's own pixel work, its wait at the
         pixel-pass barrier, its node pass, wait until the control step starts, control step, release."""

@@ -1,0 +1,331 @@
+"""Serving and batching form of the global CG solve.
+
+The reference solves one frame per ``GlobalCGSolver.solve`` call with a host
+sync per frame (d2ic/solver_global_cg.py:151-198) inside a per-sequence frame
+loop (d2ic/batch_mesh_based.py:140-225).  Here many sequences of uneven image
+and mesh sizes are served at once:
+
+* each registered sequence keeps its resident state in HBM: the reference
+  image's pixel layout (records, tables), strain tables and the warm start
+  (the previous frame's solution);
+* a request (sequence, frame image) is admitted into a free engine slot when
+  the HBM budget allows: its image is copied in (pinned -> device), its
+  B-spline coefficients are computed, and the slot is marked for admission;
+* the engine runs in slices: one persistent cooperative launch advances every
+  admitted frame by at most ``slice_rounds`` objective evaluations and keeps
+  all CG state in HBM; frames that finish free their slot, new requests join
+  at the next slice (continuous batching: work of requests that arrive while
+  others are on the GPU overlaps on the device);
+* the slice launch is captured once in a CUDA graph and replayed;
+* frames of one sequence are solved in order (frame k+1 starts from frame k's
+  solution, as BatchMeshBased with warm_start_from_previous), so a frame's
+  result is the same whether it is solved alone or in the mix: every reduction
+  inside the engine is per frame and in a fixed order.
+
+``solve_batch`` is the one-shot batched launch (all frames start together).
+"""
+from __future__ import annotations
+
+import collections
+import time
+from dataclasses import dataclass, field
+from typing import Any
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ptr
+from .dataclasses import InitMotionConfig, MeshDICConfig
+from .engine import PAD, Engine, FrameLayout, FrameSlot, as_device_image, descriptors_to_device, interp_kind
+from .mesh_assets import build_node_neighbor_tables
+from .strain import strain_device
+
+DESC_BYTES = 0
+
+
+def _desc_bytes() -> int:
+    import ctypes
+    return ctypes.sizeof(_lib.Frame)
+
+
+@dataclass
+class ServeConfig:
+    """Serving knobs: engine slots, HBM budget for admitted frames, rounds per slice, graph replay."""
+    max_slots: int = 64
+    hbm_budget_bytes: int | None = None      # default: 80% of the free device memory at start
+    slice_rounds: int = 16
+    use_graphs: bool = True
+    grid_blocks: int = 0
+
+
+@dataclass
+class Request:
+    seq_id: Any
+    frame_index: int
+    image: Any
+    t_arrival: float = 0.0
+    t_admit: float | None = None
+    t_done: float | None = None
+    u: np.ndarray | None = None
+    strain: np.ndarray | None = None
+    n_iters: int | None = None
+    status: str | None = None
+
+    @property
+    def latency(self) -> float | None:
+        return None if self.t_done is None else self.t_done - self.t_arrival
+
+
+@dataclass
+class _Sequence:
+    seq_id: Any
+    layout: FrameLayout
+    config: MeshDICConfig
+    nodes: torch.Tensor
+    strain_idx: torch.Tensor | None
+    strain_deg: torch.Tensor | None
+    u_prev: torch.Tensor | None = None
+    init: InitMotionConfig | None = None
+    centers: np.ndarray | None = None
+    in_flight: bool = False
+    queue: collections.deque = field(default_factory=collections.deque)
+    frames_done: int = 0
+
+
+class DICServer:
+    """Continuous-batching server of global-CG DIC frames on one GPU."""
+
+    def __init__(self, device=None, config: ServeConfig | None = None, interpolation: str = "cubic"):
+        self.device = torch.device(device if device is not None else "cuda")
+        self.cfg = config or ServeConfig()
+        self.kind = interp_kind(interpolation)
+        self.interpolation = interpolation
+        S = self.cfg.max_slots
+        if not 1 <= S <= _lib.MAX_FRAMES:
+            raise ValueError(f"max_slots must be in [1, {_lib.MAX_FRAMES}]")
+        self.engine = Engine(self.device, S)
+        self.cmd = self.engine.commands(S)
+        self.cmd.fill_(_lib.CMD_IDLE)
+        nb = _desc_bytes()
+        self.desc_dev = torch.zeros(S * nb, dtype=torch.uint8, device=self.device)
+        self.slots: list[tuple[FrameSlot, Request, _Sequence] | None] = [None] * S
+        self.status_dev = torch.zeros((S, 3), dtype=torch.int32, device=self.device)   # n_iters, status, n_evals
+        self.status_host = torch.zeros((S, 3), dtype=torch.int32).pin_memory()
+        self.seqs: dict[Any, _Sequence] = {}
+        self.ready: collections.deque = collections.deque()     # sequences with queued frames, FIFO
+        self.completed: list[Request] = []
+        free, _ = torch.cuda.mem_get_info(self.device)
+        self.budget = int(self.cfg.hbm_budget_bytes or 0.8 * free)
+        self.bytes_in_use = 0
+        self.copy_stream = torch.cuda.Stream(device=self.device)
+        self.graph = None
+        self.graph_failed = False
+        self.slices = 0
+        self.busy_time = 0.0
+
+    # -- sequences -----------------------------------------------------------------------------------
+    def add_sequence(self, seq_id, ref_image, mesh, assets, config: MeshDICConfig,
+                     init: InitMotionConfig | None = None, chunk_pixels: int = 256):
+        """Make a sequence resident: pixel layout of its reference image and mesh, strain tables."""
+        if seq_id in self.seqs:
+            raise ValueError(f"sequence {seq_id!r} already registered")
+        if assets.pixel_data is None:
+            raise ValueError("assets must carry pixel_data (build_pixel_assets)")
+        nn = int(np.asarray(mesh.nodes_xy).shape[0])
+        layout = FrameLayout(assets.pixel_data, nn, ref_image, self.interpolation, self.device, chunk_max=chunk_pixels)
+        T = lambda a, dt: torch.as_tensor(np.ascontiguousarray(np.asarray(a)), dtype=dt, device=self.device)
+        idx, deg = assets.node_neighbor_index, assets.node_neighbor_degree
+        if idx is None or deg is None:
+            idx, deg = build_node_neighbor_tables(mesh)
+        seq = _Sequence(seq_id, layout, config, T(mesh.nodes_xy, torch.float32), T(idx, torch.int32),
+                        T(deg, torch.int32), init=init,
+                        centers=np.asarray(assets.element_centers_xy, dtype=np.float32))
+        self.seqs[seq_id] = seq
+        self.bytes_in_use += self._layout_bytes(layout)
+        return seq
+
+    @staticmethod
+    def _layout_bytes(L: FrameLayout) -> int:
+        return int(L.pix.numel() * 4 + L.ref_image.numel() * 4 + L.chunk_begin.numel() * 4 * 4
+                   + (L.nbr_index.numel() + L.nbr_weight.numel()) * 4)
+
+    @staticmethod
+    def _slot_bytes(L: FrameLayout, max_iter: int) -> int:
+        coeff = (L.H + 2 * PAD) * L.cpitch * 4 * 2
+        ws = _lib.load().d2ic_frame_workspace_bytes(L.n_nodes, L.n_chunks, L.node_chunk_k)
+        return int(coeff + ws + L.n_nodes * 16 + max(max_iter, 1) * 12 + L.H * L.W * 4)
+
+    # -- requests ------------------------------------------------------------------------------------
+    def submit(self, req: Request):
+        seq = self.seqs[req.seq_id]
+        if not req.t_arrival:
+            req.t_arrival = time.perf_counter()
+        seq.queue.append(req)
+        if not seq.in_flight and len(seq.queue) == 1:
+            self.ready.append(seq)
+
+    def pending(self) -> int:
+        return sum(len(s.queue) for s in self.seqs.values()) + sum(x is not None for x in self.slots)
+
+    # -- scheduling ----------------------------------------------------------------------------------
+    def _admit(self):
+        free_slots = [i for i, x in enumerate(self.slots) if x is None]
+        admitted = 0
+        while free_slots and self.ready:
+            seq = self.ready[0]
+            L = seq.layout
+            need = self._slot_bytes(L, seq.config.max_iters)
+            if self.bytes_in_use + need > self.budget:
+                break                                       # wait for memory to free up
+            self.ready.popleft()
+            req = seq.queue.popleft()
+            i = free_slots.pop(0)
+            slot = FrameSlot(L, seq.config.max_iters)
+            slot.set_params(seq.config.tol, seq.config.reg_strength)
+            # image: pinned host -> device on the copy stream, then coefficients on the compute stream
+            if isinstance(req.image, torch.Tensor) and req.image.is_cuda:
+                img = req.image.to(torch.float32)
+            else:
+                src = req.image if isinstance(req.image, torch.Tensor) else torch.from_numpy(
+                    np.ascontiguousarray(req.image, dtype=np.float32))
+                img = torch.empty((L.H, L.W), dtype=torch.float32, device=self.device)
+                with torch.cuda.stream(self.copy_stream):
+                    img.copy_(src, non_blocking=True)
+                torch.cuda.current_stream(self.device).wait_stream(self.copy_stream)
+                img.record_stream(torch.cuda.current_stream(self.device))
+            slot.load_image(img)
+            if seq.u_prev is not None:
+                slot.u0.copy_(seq.u_prev)
+            elif seq.init is not None:                      # first frame: ZNCC at centres + IDW, on the device
+                from .dic_init_motion import project_centers_to_nodes_idw_device
+                from .solver_translation_zncc import match_centers_device
+                u_c, s = match_centers_device(seq.centers, L.ref_image, img, seq.init.win, seq.init.search, self.device)
+                if seq.init.score_min is not None:
+                    u_c = torch.where((s >= float(seq.init.score_min))[:, None], u_c, torch.zeros_like(u_c))
+                slot.u0.copy_(project_centers_to_nodes_idw_device(seq.nodes, seq.centers, u_c, 2.0, self.device))
+            else:
+                slot.u0.zero_()
+            # per-slot status words live in one array that is copied back after every slice
+            slot.desc.n_iters = ptr(self.status_dev[i])
+            slot.desc.status = ptr(self.status_dev[i]) + 4
+            slot.desc.n_evals = ptr(self.status_dev[i]) + 8
+            nb = _desc_bytes()
+            self.desc_dev[i * nb:(i + 1) * nb].copy_(torch.frombuffer(bytearray(bytes(slot.desc)), dtype=torch.uint8))
+            self.cmd[i] = _lib.CMD_INIT
+            self.status_dev[i, 1] = _lib.RUNNING
+            self.slots[i] = (slot, req, seq)
+            self.bytes_in_use += need
+            seq.in_flight = True
+            req.t_admit = time.perf_counter()
+            admitted += 1
+        return admitted
+
+    def _launch_slice(self):
+        n = self.cfg.max_slots
+
+        def launch():
+            self.engine.run_slice(self.desc_dev, n, self.kind, self.cfg.slice_rounds, self.cfg.grid_blocks)
+
+        if self.cfg.use_graphs and not self.graph_failed:
+            if self.graph is None:
+                try:
+                    launch()                                 # this slice runs directly; later ones replay
+                    torch.cuda.synchronize(self.device)
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g):
+                        launch()
+                    self.graph = g
+                except Exception:
+                    self.graph_failed = True
+                    self.graph = None
+                return
+            self.graph.replay()
+        else:
+            launch()
+
+    def _harvest(self):
+        self.status_host.copy_(self.status_dev, non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        now = time.perf_counter()
+        done = 0
+        for i, entry in enumerate(self.slots):
+            if entry is None:
+                continue
+            n_iters, st, _ = (int(x) for x in self.status_host[i])
+            if st == _lib.RUNNING:
+                continue
+            slot, req, seq = entry
+            u = slot.u_out
+            voigt, _ = strain_device(u, seq.nodes, seq.strain_idx, seq.strain_deg, seq.config.strain_gauge_length,
+                                     seq.config.strain_eps, self.device)
+            seq.u_prev = u.clone()
+            req.u = u.cpu().numpy()
+            req.strain = voigt.cpu().numpy()
+            req.n_iters = n_iters
+            req.status = _lib.STATUS_NAMES.get(st, str(st))
+            req.t_done = now
+            self.completed.append(req)
+            self.slots[i] = None
+            self.cmd[i] = _lib.CMD_IDLE
+            self.bytes_in_use -= self._slot_bytes(seq.layout, seq.config.max_iters)
+            seq.in_flight = False
+            seq.frames_done += 1
+            if seq.queue:
+                self.ready.append(seq)
+            done += 1
+        return done
+
+    def step(self) -> int:
+        """Admit what fits, run one engine slice, harvest finished frames; returns frames completed."""
+        self._admit()
+        if all(x is None for x in self.slots):
+            return 0
+        t0 = time.perf_counter()
+        self._launch_slice()                        # the kernel turns CMD_INIT into CMD_RUN as it admits
+        done = self._harvest()
+        self.busy_time += time.perf_counter() - t0
+        self.slices += 1
+        return done
+
+    def run_until_idle(self):
+        while self.pending():
+            self.step()
+        return self.completed
+
+    def stats(self) -> dict:
+        lat = np.array([r.latency for r in self.completed if r.latency is not None])
+        out = {"frames": len(self.completed), "slices": self.slices, "graphs": self.graph is not None}
+        if lat.size:
+            out.update(latency_ms_p50=1000 * float(np.percentile(lat, 50)),
+                       latency_ms_p99=1000 * float(np.percentile(lat, 99)))
+        return out
+
+
+def solve_batch(frames, device=None, grid_blocks: int = 0):
+    """One batched persistent launch over independent frames.
+
+    ``frames``: list of ``(layout, def_image, u0, MeshDICConfig)``.  Returns a
+    list of ``(u (Nn,2) numpy, n_iters, status, history numpy)``.
+    """
+    device = torch.device(device if device is not None else "cuda")
+    slots = []
+    for L, img, u0, cfg in frames:
+        s = FrameSlot(L, cfg.max_iters)
+        s.set_params(cfg.tol, cfg.reg_strength)
+        s.load_image(img)
+        s.set_u0(u0)
+        slots.append(s)
+    kinds = {s.layout.kind for s in slots}
+    if len(kinds) != 1:
+        raise ValueError("one batched launch uses one interpolation kind")
+    eng = Engine(device, len(slots))
+    desc = descriptors_to_device([s.desc for s in slots], device)
+    eng.solve(desc, len(slots), kinds.pop(), grid_blocks)
+    torch.cuda.synchronize(device)
+    out = []
+    for s in slots:
+        info = s.info.cpu().tolist()
+        out.append((s.u_out.cpu().numpy(), info[0], _lib.STATUS_NAMES.get(info[1], str(info[1])),
+                    s.hist.cpu().numpy()))
+    return out

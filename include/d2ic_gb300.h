@@ -37,6 +37,7 @@ extern "C" {
 #define D2IC_WAIT_TIMEOUT  -5   /* a bounded device-side wait gave up         */
 #define D2IC_CUDA_ERROR    -6
 #define D2IC_UNSUPPORTED   -7
+#define D2IC_RUNNING        1   /* per-frame status: not finished at the end of a slice */
 
 /* interpolation kinds (GlobalCGSolver(interpolation=...)) */
 #define D2IC_INTERP_CUBIC   0   /* cubic B-spline, edge-replicating boundary  */
@@ -147,6 +148,22 @@ D2IC_API size_t d2ic_cg_control_bytes(int n_frames);
  * descriptor's u_out / hist / n_iters / status. */
 D2IC_API int d2ic_cg_solve_batched(const d2ic_frame_t *frames, int n_frames, void *control,
                           size_t control_bytes, int interp_kind, int grid_blocks, void *stream);
+
+/* Continuous batching: run at most max_rounds objective evaluations ("rounds")
+ * of the frames in `frames`, keeping every frame's CG state in `control`
+ * between calls.  Before a call the host sets one command word per frame at
+ * control + d2ic_cg_command_offset(): D2IC_CMD_INIT admits a new frame (u0,
+ * image coefficients and outputs must be ready), D2IC_CMD_RUN continues (or
+ * leaves finished frames alone), D2IC_CMD_IDLE parks an empty slot.  A frame
+ * that finishes during the call gets its outputs and final status written;
+ * unfinished frames report D2IC_RUNNING.  Serves the batched/served form of
+ * GlobalCGSolver.solve (d2ic/solver_global_cg.py:151-198) for many frames. */
+#define D2IC_CMD_INIT 0
+#define D2IC_CMD_RUN  1
+#define D2IC_CMD_IDLE 2
+D2IC_API size_t d2ic_cg_command_offset(void);
+D2IC_API int d2ic_cg_slice(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
+                           int interp_kind, int grid_blocks, int max_rounds, void *stream);
 
 /* As d2ic_cg_solve_batched, and writes 6 %globaltimer stamps per round into
  * trace[6*r .. 6*r+5] for r < trace_rounds: block 0's round start, end of the

@@ -1,0 +1,95 @@
+"""Batched and served solves against the plain single-frame path (GPU).
+
+Every reduction in the engine is per frame and in a fixed order, so a frame's
+result must be bitwise the same alone, in a batch of uneven frames, and when
+it is admitted into a running server and advanced across several slices.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(H, elem, warp, seed, mask_frac=0.85):
+    import d2ic_gb300 as d2
+    from d2ic_gb300.synthetic import rect_mask, speckle_sequence
+    ref, frames = speckle_sequence(H, H, [warp], seed=seed, noise_seeds=[seed, seed + 1])
+    side = int(H * mask_frac)
+    mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, H, side, side), elem)
+    pix = d2.build_pixel_assets(mesh, ref, 1.0, assets.roi_mask)
+    return ref, frames[0], mesh, assets, pix
+
+
+@pytest.fixture(scope="module")
+def uneven(cuda):
+    from d2ic_gb300.synthetic import Affine, Translation
+    return [
+        _case(192, 12, Translation(0.4, -0.3), 21),
+        _case(256, 16, Affine([[0.01, 0.002], [-0.001, -0.008]], [0.6, 0.2], [128, 128]), 22),
+        _case(320, 24, Translation(-0.7, 0.5), 23),
+    ]
+
+
+def test_batch_alone_equals_mix(cuda, uneven):
+    import d2ic_gb300 as d2
+    from d2ic_gb300 import engine
+    from d2ic_gb300.serving import solve_batch
+    cfg = d2.MeshDICConfig(max_iters=80, tol=1e-4, reg_strength=0.1)
+    items = []
+    for ref, dfm, mesh, assets, pix in uneven:
+        L = engine.FrameLayout(pix, mesh.nodes_xy.shape[0], ref, "cubic", cuda)
+        items.append((L, dfm, None, cfg))
+    alone = [solve_batch([it], cuda)[0] for it in items]
+    mixed = solve_batch(items, cuda)
+    for a, m in zip(alone, mixed):
+        assert a[1] == m[1] and a[2] == m[2]
+        assert np.array_equal(a[0], m[0])                      # bitwise
+        assert np.array_equal(a[3], m[3], equal_nan=True)
+
+
+def test_server_equals_plain_sequences(cuda):
+    """Two sequences, three frames each, interleaved; frames cross several engine slices."""
+    import d2ic_gb300 as d2
+    from d2ic_gb300.serving import DICServer, Request, ServeConfig
+    from d2ic_gb300.synthetic import Translation, rect_mask, speckle_sequence
+    seqs = {}
+    for sid, (H, elem, seed) in enumerate([(192, 16, 31), (256, 12, 32)]):
+        warps = [Translation(0.2 * (k + 1), -0.15 * (k + 1)) for k in range(3)]
+        ref, frames = speckle_sequence(H, H, warps, seed=seed, noise_seeds=[seed, seed + 1, seed + 2, seed + 3])
+        mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, H, H - 32, H - 32), elem)
+        from dataclasses import replace
+        assets = replace(assets, pixel_data=d2.build_pixel_assets(mesh, ref, 1.0, assets.roi_mask))
+        seqs[sid] = (ref, frames, mesh, assets)
+    cfg = d2.MeshDICConfig(max_iters=60, tol=1e-4, reg_strength=0.1)
+    # plain: one DICMeshBased per sequence, frame by frame, warm start from the previous frame
+    plain = {}
+    for sid, (ref, frames, mesh, assets) in seqs.items():
+        dic = d2.DICMeshBased(mesh, d2.GlobalCGSolver(), cfg)
+        dic.prepare(ref, assets)
+        u_prev, out = None, []
+        for f in frames:
+            if u_prev is not None:
+                dic.set_initial_guess(u_prev)
+            r = dic.run(f)
+            out.append(r)
+            u_prev = r.u_nodal
+        plain[sid] = out
+    # served: both sequences at once, slices of 7 rounds
+    srv = DICServer(cuda, ServeConfig(max_slots=4, slice_rounds=7))
+    for sid, (ref, frames, mesh, assets) in seqs.items():
+        srv.add_sequence(sid, ref, mesh, assets, cfg)
+    for k in range(3):
+        for sid, (ref, frames, mesh, assets) in seqs.items():
+            srv.submit(Request(sid, k, frames[k]))
+    done = srv.run_until_idle()
+    assert len(done) == 6
+    assert srv.slices > 3
+    for r in done:
+        p = plain[r.seq_id][r.frame_index]
+        assert r.n_iters == p.diagnostics.info["n_iters"]
+        assert np.array_equal(r.u, np.asarray(p.u_nodal))      # bitwise, alone vs in the mix
+        assert np.abs(r.strain - np.asarray(p.strain)).max() <= 1e-6
+    st = srv.stats()
+    assert st["frames"] == 6 and st["latency_ms_p99"] >= st["latency_ms_p50"] > 0
