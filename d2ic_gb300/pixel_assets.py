@@ -172,31 +172,49 @@ def _solve2(a11, a12, a21, a22, b1, b2):
     return x1, x2
 
 
+def _newton_step(xi, eta, X, Y, px, py):
+    om_x, op_x, om_e, op_e = 1 - xi, 1 + xi, 1 - eta, 1 + eta
+    n0 = 0.25 * om_x * om_e
+    n1 = 0.25 * op_x * om_e
+    n2 = 0.25 * op_x * op_e
+    n3 = 0.25 * om_x * op_e
+    dx0, dx1, dx2, dx3 = -0.25 * om_e, 0.25 * om_e, 0.25 * op_e, -0.25 * op_e
+    de0, de1, de2, de3 = -0.25 * om_x, -0.25 * op_x, 0.25 * op_x, 0.25 * om_x
+    X0, X1, X2, X3 = X
+    Y0, Y1, Y2, Y3 = Y
+    fx = (((n0 * X0 + n1 * X1) + n2 * X2) + n3 * X3) - px
+    fy = (((n0 * Y0 + n1 * Y1) + n2 * Y2) + n3 * Y3) - py
+    j11 = ((dx0 * X0 + dx1 * X1) + dx2 * X2) + dx3 * X3
+    j21 = ((dx0 * Y0 + dx1 * Y1) + dx2 * Y2) + dx3 * Y3
+    j12 = ((de0 * X0 + de1 * X1) + de2 * X2) + de3 * X3
+    j22 = ((de0 * Y0 + de1 * Y1) + de2 * Y2) + de3 * Y3
+    return _solve2(j11, j12, j21, j22, fx, fy)
+
+
 def local_coordinates(pixel_coords, pixel_nodes, nodes_coord, iters: int = 10):
-    """(xi, eta) of each pixel in its element by Newton from (0,0) (d2ic/pixel_assets.py:277-294)."""
+    """(xi, eta) of each pixel in its element by Newton from (0,0) (d2ic/pixel_assets.py:277-294).
+
+    A pixel whose update is exactly zero keeps (xi, eta), so every later
+    iteration repeats the same zero update: such pixels drop out of the
+    remaining iterations, which gives bit-for-bit the result of all ``iters``
+    steps at a fraction of the cost (axis-aligned elements settle in 2-3).
+    """
     pc = np.asarray(pixel_coords, dtype=np.float64)
     Xe = np.asarray(nodes_coord, dtype=np.float64)[np.asarray(pixel_nodes)]
-    X0, X1, X2, X3 = (Xe[:, a, 0] for a in range(4))
-    Y0, Y1, Y2, Y3 = (Xe[:, a, 1] for a in range(4))
-    xi = np.zeros(pc.shape[0])
-    eta = np.zeros(pc.shape[0])
+    n = pc.shape[0]
+    xi = np.zeros(n)
+    eta = np.zeros(n)
+    live = np.arange(n)
     for _ in range(iters):
-        om_x, op_x, om_e, op_e = 1 - xi, 1 + xi, 1 - eta, 1 + eta
-        n0 = 0.25 * om_x * om_e
-        n1 = 0.25 * op_x * om_e
-        n2 = 0.25 * op_x * op_e
-        n3 = 0.25 * om_x * op_e
-        dx0, dx1, dx2, dx3 = -0.25 * om_e, 0.25 * om_e, 0.25 * op_e, -0.25 * op_e
-        de0, de1, de2, de3 = -0.25 * om_x, -0.25 * op_x, 0.25 * op_x, 0.25 * om_x
-        fx = (((n0 * X0 + n1 * X1) + n2 * X2) + n3 * X3) - pc[:, 0]
-        fy = (((n0 * Y0 + n1 * Y1) + n2 * Y2) + n3 * Y3) - pc[:, 1]
-        j11 = ((dx0 * X0 + dx1 * X1) + dx2 * X2) + dx3 * X3
-        j21 = ((dx0 * Y0 + dx1 * Y1) + dx2 * Y2) + dx3 * Y3
-        j12 = ((de0 * X0 + de1 * X1) + de2 * X2) + de3 * X3
-        j22 = ((de0 * Y0 + de1 * Y1) + de2 * Y2) + de3 * Y3
-        d1, d2 = _solve2(j11, j12, j21, j22, fx, fy)
-        xi = xi - d1
-        eta = eta - d2
+        if live.size == 0:
+            break
+        X = tuple(Xe[live, a, 0] for a in range(4))
+        Y = tuple(Xe[live, a, 1] for a in range(4))
+        d1, d2 = _newton_step(xi[live], eta[live], X, Y, pc[live, 0], pc[live, 1])
+        xi[live] = xi[live] - d1
+        eta[live] = eta[live] - d2
+        moving = (d1 != 0) | (d2 != 0) | ~np.isfinite(d1) | ~np.isfinite(d2)
+        live = live[moving]
     return xi, eta
 
 
