@@ -55,6 +55,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-sample-frames", type=int, default=2)
+    p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--serve-seqs", type=int, default=16)
+    p.add_argument("--serve-frames", type=int, default=4)
+    p.add_argument("--serve-slots", type=int, default=32)
+    p.add_argument("--serve-slice", type=int, default=16)
     return p.parse_args()
 
 
@@ -216,6 +221,96 @@ def run_reference(args, ws, rank):
 
 
 # ---------------------------------------------------------------------------
+# served vs plain on a mixed stream
+# ---------------------------------------------------------------------------
+
+def run_serving(args, dev):
+    """Plain single-frame drop-in vs the continuous-batching server on the same requests."""
+    import torch
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300 import workloads
+    from d2ic_gb300.serving import DICServer, Request, ServeConfig
+
+    seqs = workloads.mixed_stream(n_seq=args.serve_seqs, frames_per_seq=args.serve_frames, device=dev)
+    F = args.serve_frames
+    order = [(s, k) for k in range(F) for s in range(len(seqs))]
+    pinned = [[torch.from_numpy(f).pin_memory() for f in wl.frames] for wl in seqs]
+    n_pix = sum(wl.n_pix for wl in seqs) * F
+
+    # plain: the reference's per-frame pipeline on our drop-in (one launch + host sync per frame)
+    dics, inits = [], []
+    for wl in seqs:
+        dic = d2.DICMeshBased(wl.mesh, d2.GlobalCGSolver(device=dev), wl.config)
+        dic.prepare(wl.ref, wl.assets)
+        ini = d2.DICInitMotion(wl.init, d2.TranslationZNCCSolver(wl.init, device=dev))
+        ini.prepare(wl.ref, dic.state.assets)
+        dics.append(dic)
+        inits.append(ini)
+
+    def plain_pass():
+        prev = [None] * len(seqs)
+        out, lat = {}, []
+        for s, k in order:
+            t0 = time.perf_counter()
+            if k == 0:
+                dics[s].set_initial_guess(inits[s].run(pinned[s][0]).u_nodal)
+            else:
+                dics[s].set_initial_guess(prev[s])
+            r = dics[s].run(pinned[s][k])
+            prev[s] = r.u_nodal
+            out[(s, k)] = np.asarray(r.u_nodal)
+            lat.append(time.perf_counter() - t0)
+        return out, lat
+
+    plain_pass()                                         # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_u, plain_lat = plain_pass()
+    t_plain = time.perf_counter() - t0
+
+    srv = DICServer(dev, ServeConfig(max_slots=args.serve_slots, slice_rounds=args.serve_slice))
+    for s, wl in enumerate(seqs):
+        srv.add_sequence(s, wl.ref, wl.mesh, wl.assets, wl.config, init=wl.init)
+
+    def served_pass(offsets=None):
+        srv.reset_sequences()
+        reqs = [Request(s, k, pinned[s][k]) for s, k in order]
+        if offsets is None:
+            t = time.perf_counter()
+            for r in reqs:
+                r.t_arrival = t
+                srv.submit(r)
+            srv.run_until_idle()
+        else:
+            srv.run_stream(reqs, offsets)
+        return reqs
+
+    served_pass()                                        # warm-up (graph capture)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reqs = served_pass()
+    t_served = time.perf_counter() - t0
+    diff = max(float(np.abs(r.u - plain_u[(r.seq_id, r.frame_index)]).max()) for r in reqs)
+    served_fps = len(reqs) / t_served
+    # online: Poisson arrivals at half the measured served throughput
+    rate = 0.5 * served_fps
+    rng = np.random.default_rng(4)
+    offsets = np.cumsum(rng.exponential(1.0 / rate, len(order)))
+    reqs_on = served_pass(offsets)
+    lat = np.array([r.latency for r in reqs_on])
+    return {"workload": "mixed_stream", "sequences": len(seqs), "frames": len(order),
+            "image_sides": sorted({int(wl.ref.shape[0]) for wl in seqs}), "roi_pixels_per_pass": int(n_pix),
+            "plain_frames_per_s": len(order) / t_plain, "served_frames_per_s": served_fps,
+            "speedup": served_fps / (len(order) / t_plain), "max_abs_diff_vs_plain_px": diff,
+            "plain_latency_ms_p50": 1000 * float(np.percentile(plain_lat, 50)),
+            "plain_latency_ms_p99": 1000 * float(np.percentile(plain_lat, 99)),
+            "online_rate_frames_per_s": rate, "latency_ms_p50": 1000 * float(np.percentile(lat, 50)),
+            "latency_ms_p99": 1000 * float(np.percentile(lat, 99)), "slots": args.serve_slots,
+            "slice_rounds": args.serve_slice, "graphs": srv.graph is not None}
+
+
+# ---------------------------------------------------------------------------
 # GPU leg
 # ---------------------------------------------------------------------------
 
@@ -325,6 +420,9 @@ def run_ours(args, ws, rank, local):
         u_dev = res.u.cpu().numpy()
         u_api = np.stack([np.asarray(r.u_nodal) for r in res_b.results])
         out["e2e"]["max_abs_diff_vs_value_path_px"] = float(np.abs(u_dev - u_api).max())
+
+    if not args.no_serve:
+        out["serving"] = run_serving(args, dev)
 
     if not args.no_cpu and rank == 0:
         cb = cpu_sequence_sample(wl, args.cpu_sample_frames, u_start=res.u[0].cpu().numpy())

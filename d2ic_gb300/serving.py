@@ -165,6 +165,35 @@ class DICServer:
         if not seq.in_flight and len(seq.queue) == 1:
             self.ready.append(seq)
 
+    def reset_sequences(self):
+        """Forget warm starts and completed requests (resident layouts are kept)."""
+        if any(x is not None for x in self.slots):
+            raise RuntimeError("reset while frames are in flight")
+        for s in self.seqs.values():
+            s.u_prev = None
+            s.queue.clear()
+            s.in_flight = False
+            s.frames_done = 0
+        self.ready.clear()
+        self.completed = []
+
+    def run_stream(self, requests, offsets):
+        """Online serving: request i arrives ``offsets[i]`` seconds after the call (sorted)."""
+        t0 = time.perf_counter()
+        i = 0
+        n = len(requests)
+        while i < n or self.pending():
+            now = time.perf_counter() - t0
+            while i < n and offsets[i] <= now:
+                requests[i].t_arrival = t0 + offsets[i]
+                self.submit(requests[i])
+                i += 1
+            if self.pending():
+                self.step()
+            elif i < n:
+                time.sleep(max(0.0, offsets[i] - (time.perf_counter() - t0)))
+        return self.completed
+
     def pending(self) -> int:
         return sum(len(s.queue) for s in self.seqs.values()) + sum(x is not None for x in self.slots)
 

@@ -56,6 +56,44 @@ def translation_512(seed: int = 0, device="cpu") -> Workload:
                     MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1), None, [warp])
 
 
+def mixed_stream(n_seq: int = 16, frames_per_seq: int = 4, seed: int = 4, device="cpu",
+                 sides=(512, 1024, 2048), elements=(8, 16, 32)):
+    """Sequences of uneven size for the served form (seed ``seed``; sequence s uses ``4000 + s``).
+
+    Per sequence: side and element size drawn uniformly, ellipse mask covering
+    40-90%, a random affine map (strains +-2%, rotation +-1 deg, translation
+    +-3 px) reached progressively (frame k at fraction (k+1)/frames_per_seq),
+    N(0, 0.5^2) grey noise per image; frame 0 is initialised by ZNCC + IDW.
+    """
+    import math
+    from dataclasses import replace
+
+    from .synthetic import Affine, ellipse_mask
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(n_seq):
+        H = int(rng.choice(sides))
+        elem = int(rng.choice(elements))
+        r = np.random.default_rng(4000 + s)
+        exx, eyy, exy = r.uniform(-0.02, 0.02, 3)
+        th = math.radians(r.uniform(-1.0, 1.0))
+        t = r.uniform(-3.0, 3.0, 2)
+        A = np.array([[exx, exy], [exy, eyy]]) + np.array([[math.cos(th) - 1, -math.sin(th)],
+                                                          [math.sin(th), math.cos(th) - 1]])
+        warps = [Affine(A * (k + 1) / frames_per_seq, t * (k + 1) / frames_per_seq, [H / 2, H / 2])
+                 for k in range(frames_per_seq)]
+        ref, frames = speckle_sequence(H, H, warps, seed=4000 + s, noise_seeds=[40000 + 100 * s + k for k in
+                                                                                 range(frames_per_seq + 1)],
+                                       noise_sigma=0.5, device=device)
+        mask = ellipse_mask(H, H, r)
+        mesh, assets = mask_to_mesh_assets(mask, elem)
+        assets = replace(assets, pixel_data=build_pixel_assets(mesh, ref, 1.0, assets.roi_mask))
+        out.append(Workload(f"seq{s}_{H}px_e{elem}", ref, frames, mask, mesh, assets,
+                            MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1),
+                            InitMotionConfig(win=17, search=8, score_min=0.2), warps))
+    return out
+
+
 def plate_hole_2048(n_frames: int = 20, seed: int = 1, device="cpu", H: int = 2048) -> Workload:
     W = H
     s = H / 2048.0
