@@ -54,10 +54,21 @@ def test_gpu_path_against_golden(cuda, gold):
     dic.prepare(gold["ref"], assets)
     res = dic.run(gold["deformed"])
     used = np.unique(gold["elements"])
-    err = np.abs(np.asarray(res.u_nodal, np.float64)[used] - gold["u_conv"][used]).max()
+    u = np.asarray(res.u_nodal, np.float64)
+    err = np.abs(u[used] - gold["u_conv"][used]).max()
     assert err <= 1e-3, err                                                    # nodal tolerance, px
     assert abs(res.diagnostics.info["n_iters"] - int(gold["k_conv"])) <= 2
-    assert np.abs(np.asarray(res.strain) - gold["strain_voigt"]).max() <= 1e-5   # strain tolerance
+    # strain kernel parity: the GPU strain against the FP64 strain of the GPU's own displacement
+    from oracle import mesh as om, strain as ostrain
+    sidx, sdeg = om.node_neighbor_tables(gold["nodes"], gold["elements"])
+    _, E = ostrain.green_lagrange_nodes_lsq(u, gold["nodes"], sidx, sdeg)
+    assert np.abs(np.asarray(res.strain) - ostrain.to_voigt(E)).max() <= 1e-5   # strain tolerance
+    # end to end: the two solves stop at tol 1e-3 within an iteration or two of each other; a strain is a
+    # difference quotient of nodal values over the 16 px element, so its gap is bounded by ~2 err / 16
+    e2e = np.abs(np.asarray(res.strain) - gold["strain_voigt"]).max()
+    print(f"golden: n_iters gpu={res.diagnostics.info['n_iters']} oracle={int(gold['k_conv'])} "
+          f"max|du|={err:.2e} px max|dE|={e2e:.2e}")
+    assert e2e <= 1e-5 + 2 * err / 16
     J, g = dic.solver.objective_and_gradient(dic.state, gold["deformed"], gold["u_rand"])
     assert abs(J - float(gold["J1"])) <= 1e-5 * abs(float(gold["J1"]))
     assert np.abs(g - gold["g1"]).max() <= 1e-4 * np.abs(gold["g1"]).max()
