@@ -76,7 +76,12 @@ _SIGS = {
     "d2ic_cg_command_offset": (szt, []),
     "d2ic_cg_slice": (i32, [vp, i32, vp, szt, i32, i32, i32, vp]),
     "d2ic_eval_objective": (i32, [vp, vp, vp, szt, i32, vp, vp, vp]),
-    "d2ic_zncc_match": (i32, [vp, i32, i32, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp]),
+    "d2ic_hessian_chunks": (i32, [vp, i32, vp, i32, vp, vp]),
+    "d2ic_hessian_matvec": (i32, [vp, i32, i32, vp, vp, i32, f32, f32, vp, vp, vp]),
+    "d2ic_mixed_term": (i32, [vp, i32, i32, vp, vp, f32, vp, vp, i32, i32, vp]),
+    "d2ic_mixed_term_T": (i32, [vp, i32, vp, vp, f32, vp, vp]),
+    "d2ic_bspline_prefilter_T": (i32, [vp, i32, i32, i32, i32, vp, vp, vp]),
+    "d2ic_zncc_match":(i32, [vp, i32, i32, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp]),
     "d2ic_idw_project": (i32, [vp, i32, vp, vp, i32, f32, vp, vp]),
     "d2ic_strain_gl": (i32, [vp, vp, vp, vp, i32, i32, f32, f32, vp, vp, vp]),
 }

@@ -1,0 +1,257 @@
+"""Implicit-function adjoint of the converged global-CG solve.
+
+The reference propagates image noise with ``jax.jvp`` through 25 unrolled
+iterations of its nonlinear CG (doc/11_Advanced_Use_Uncertainty_Propagation.ipynb,
+cells 14, 22, 24, 30).  Here the derivative of the converged solution u*(I2)
+(grad_u J(u*, I2) = 0) is taken by the implicit function theorem:
+
+    du* = -H^-1 (d grad_u J / dI2) dI,         dL/dI2 = -(d grad_u J / dI2)^T H^-1 dL/du*,
+
+with H the exact Hessian of J at u* (pixel term with the residual times the
+image Hessian, plus springs).  All heavy pieces are CUDA kernels of the
+library: one pixel pass assembles per-chunk element blocks of H, H V for many
+right-hand sides runs on those blocks (chunk -> slot -> node, no atomics), the
+mixed term is a pixel pass over an image direction's B-spline coefficients and
+its adjoint is the backward of the bicubic sampling (scatter + transposed
+prefilter).  The right-hand sides of all noise realisations are solved
+together by a block-Jacobi preconditioned CG (FP64 vectors, FP32 matvec).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ptr
+from .engine import PAD, Engine, FrameLayout, FrameSlot, descriptors_to_device, prepare_coefficients
+
+
+def _pair(a, b):
+    a, b = min(a, b), max(a, b)
+    return a * 4 - (a * (a - 1)) // 2 + (b - a)
+
+
+class ImplicitAdjoint:
+    """Linearisation of one converged frame: JVP and VJP with respect to the deformed image."""
+
+    def __init__(self, slot: FrameSlot, u_star, alpha_reg: float, exact: bool = True, stream=None):
+        L: FrameLayout = slot.layout
+        if L.kind != _lib.INTERP_CUBIC:
+            raise ValueError("the adjoint is implemented for cubic interpolation")
+        self.slot, self.L = slot, L
+        self.dev = L.device
+        self.alpha = float(alpha_reg)
+        self.inv_np = 1.0 / max(L.n_pix, 1)
+        self.u = torch.as_tensor(u_star, dtype=torch.float32, device=self.dev).reshape(-1, 2).contiguous()
+        self.desc = descriptors_to_device([slot.desc], self.dev)
+        self.hess = torch.empty(max(L.n_chunks, 1) * 32, dtype=torch.float32, device=self.dev)
+        _lib.call("d2ic_hessian_chunks", ptr(self.desc), L.n_chunks, ptr(self.u), int(exact), ptr(self.hess),
+                  _lib.stream_handle(stream))
+        self._precond()
+        self._slots_cap = 0
+        self._slots = None
+
+    # -- preconditioner: inverse 2x2 diagonal blocks, inactive dofs masked -------------------------------
+    def _precond(self):
+        L = self.L
+        h = self.hess.cpu().numpy().reshape(-1, 32)[: L.n_chunks]
+        cn = L.chunk_nodes.cpu().numpy().reshape(-1, 4)
+        D = np.zeros((L.n_nodes, 3))
+        for a in range(4):
+            k = 3 * _pair(a, a)
+            np.add.at(D, cn[:, a], h[:, k:k + 3] * self.inv_np)
+        nbi = L.nbr_index.cpu().numpy().reshape(L.max_deg, L.n_nodes) if L.max_deg else np.zeros((0, L.n_nodes), int)
+        nbw = L.nbr_weight.cpu().numpy().reshape(L.max_deg, L.n_nodes) if L.max_deg else np.zeros((0, L.n_nodes))
+        spring = np.where(nbi >= 0, nbw, 0.0).sum(axis=0)
+        D[:, 0] += self.alpha * spring
+        D[:, 2] += self.alpha * spring
+        det = D[:, 0] * D[:, 2] - D[:, 1] ** 2
+        active = (np.abs(D).sum(axis=1) > 0) & (det > 0)
+        inv = np.zeros((L.n_nodes, 2, 2))
+        inv[active, 0, 0] = D[active, 2] / det[active]
+        inv[active, 1, 1] = D[active, 0] / det[active]
+        inv[active, 0, 1] = inv[active, 1, 0] = -D[active, 1] / det[active]
+        self.Minv = torch.as_tensor(inv, dtype=torch.float64, device=self.dev)
+        self.active = torch.as_tensor(active, device=self.dev)
+
+    def matvec(self, V: torch.Tensor) -> torch.Tensor:
+        """H V for V of shape (Nn, 2, K) (float64 in, float64 out; the kernels run in FP32)."""
+        L = self.L
+        K = V.shape[2]
+        Vf = V.to(torch.float32).contiguous()
+        need = L.node_chunk_k * L.n_nodes * 2 * K
+        if need > self._slots_cap:
+            self._slots = torch.empty(need, dtype=torch.float32, device=self.dev)
+            self._slots_cap = need
+        Y = torch.empty_like(Vf)
+        _lib.call("d2ic_hessian_matvec", ptr(self.desc), L.n_chunks, L.n_nodes, ptr(self.hess), ptr(Vf), K,
+                  self.inv_np, self.alpha, ptr(self._slots), ptr(Y), _lib.stream_handle())
+        return Y.to(torch.float64)
+
+    def solve(self, B: torch.Tensor, rtol: float = 1e-7, max_iter: int = 2000):
+        """X = H^-1 B column by column (block-Jacobi PCG, all columns in lock step)."""
+        B = B.to(torch.float64)
+        mask = self.active[:, None, None].to(B.dtype)
+        B = B * mask
+        X = torch.zeros_like(B)
+        R = B.clone()
+        Z = torch.einsum("nij,njk->nik", self.Minv, R)
+        P = Z.clone()
+        rz = (R * Z).sum(dim=(0, 1))
+        bn = torch.sqrt((B * B).sum(dim=(0, 1))).clamp_min(1e-300)
+        it = 0
+        for it in range(1, max_iter + 1):
+            AP = self.matvec(P) * mask
+            pap = (P * AP).sum(dim=(0, 1))
+            a = torch.where(pap > 0, rz / pap, torch.zeros_like(rz))
+            X += P * a
+            R -= AP * a
+            rn = torch.sqrt((R * R).sum(dim=(0, 1)))
+            if bool((rn <= rtol * bn).all()):
+                break
+            Z = torch.einsum("nij,njk->nik", self.Minv, R)
+            rz_new = (R * Z).sum(dim=(0, 1))
+            P = Z + P * torch.where(rz > 0, rz_new / rz, torch.zeros_like(rz))
+            rz = rz_new
+        self.last_iters = it
+        return X
+
+    # -- the mixed term and its adjoint ---------------------------------------------------------------
+    def _coeff(self, img: torch.Tensor) -> torch.Tensor:
+        return prepare_coefficients(img.to(torch.float32).contiguous(), _lib.INTERP_CUBIC)
+
+    def mixed(self, dI: torch.Tensor) -> torch.Tensor:
+        """(d grad_u J / dI2) dI_k for images dI (K, H, W) -> (Nn, 2, K)."""
+        L = self.L
+        K = dI.shape[0]
+        out = torch.empty((L.n_nodes, 2, K), dtype=torch.float32, device=self.dev)
+        slots = torch.zeros(L.node_chunk_k * L.n_nodes * 2, dtype=torch.float32, device=self.dev)
+        for k in range(K):
+            c = self._coeff(dI[k])
+            _lib.call("d2ic_mixed_term", ptr(self.desc), L.n_chunks, L.n_nodes, ptr(self.u), ptr(c), self.inv_np,
+                      ptr(slots), ptr(out), K, k, _lib.stream_handle())
+        return out.to(torch.float64)
+
+    def mixed_T(self, lam: torch.Tensor) -> torch.Tensor:
+        """Adjoint: (Nn, 2, K) -> image-space (K, H, W)."""
+        L = self.L
+        K = lam.shape[2]
+        out = torch.empty((K, L.H, L.W), dtype=torch.float32, device=self.dev)
+        gco = torch.empty((L.H + 2 * PAD, L.cpitch), dtype=torch.float32, device=self.dev)
+        tmp = torch.empty((L.H, L.cpitch), dtype=torch.float32, device=self.dev)
+        for k in range(K):
+            lk = lam[:, :, k].to(torch.float32).contiguous()
+            gco.zero_()
+            _lib.call("d2ic_mixed_term_T", ptr(self.desc), L.n_chunks, ptr(self.u), ptr(lk), self.inv_np, ptr(gco),
+                      _lib.stream_handle())
+            _lib.call("d2ic_bspline_prefilter_T", ptr(gco), L.H, L.W, PAD, L.cpitch, ptr(tmp), ptr(out[k]),
+                      _lib.stream_handle())
+        return out
+
+    def jvp(self, dI: torch.Tensor, **kw) -> torch.Tensor:
+        """du*/dI2 . dI for images (K, H, W) -> (K, Nn, 2)."""
+        X = self.solve(self.mixed(dI), **kw)
+        return (-X).permute(2, 0, 1).contiguous()
+
+    def vjp(self, gu: torch.Tensor, **kw) -> torch.Tensor:
+        """(du*/dI2)^T gu for gu (K, Nn, 2) -> (K, H, W)."""
+        lam = self.solve(gu.to(torch.float64).permute(1, 2, 0).contiguous(), **kw)
+        return -self.mixed_T(lam)
+
+
+def newton_polish(solver, state, def_image, u, alpha_reg: float, steps: int = 3, exact: bool = True):
+    """Refine a CG solution with exact Newton steps u <- u - H^-1 grad J (on the GPU)."""
+    slot = solver._ensure(state)
+    slot.load_image(def_image)
+    u = torch.as_tensor(u, dtype=torch.float32, device=slot.layout.device).reshape(-1, 2).contiguous()
+    for _ in range(steps):
+        _, g = solver._engine.eval_objective(solver._desc_dev, u, solver._kind)
+        adj = ImplicitAdjoint(slot, u, alpha_reg, exact)
+        step = adj.solve(g.to(torch.float64).reshape(-1, 2, 1))[:, :, 0]
+        u = (u.to(torch.float64) - step).to(torch.float32).contiguous()
+    return u
+
+
+def strain_jvp(u, du, nodes, nbr_index, nbr_degree, gauge_length: float = 0.0, eps: float = 1e-8):
+    """Linearised Green-Lagrange Voigt strain: d voigt for displacement directions du (K, Nn, 2).
+
+    Same weighted least squares as d2ic/strain.py:11-92 (FP64 torch), differentiated:
+    G = A^-1 B(u), dE = (dG^T F + F^T dG) / 2 with F = I + G.
+    """
+    dev = du.device
+    u = torch.as_tensor(u, dtype=torch.float64, device=dev).reshape(-1, 2)
+    X = torch.as_tensor(np.asarray(nodes), dtype=torch.float64, device=dev).reshape(-1, 2)
+    idx = torch.as_tensor(np.asarray(nbr_index), dtype=torch.long, device=dev)
+    deg = torch.as_tensor(np.asarray(nbr_degree), dtype=torch.long, device=dev)
+    n, md = idx.shape
+    mask = torch.arange(md, device=dev)[None, :] < deg[:, None]
+    nid = torch.where(mask, idx, torch.zeros_like(idx))
+    dX = X[nid] - X[:, None, :]
+    w = mask.to(torch.float64)
+    if gauge_length > 0:
+        r = torch.linalg.norm(dX, dim=2)
+        w = w * torch.exp(-(r / (gauge_length + 1e-12)) ** 2)
+    A = torch.einsum("nk,nki,nkj->nij", w, dX, dX) + eps * torch.eye(2, dtype=torch.float64, device=dev)
+    Ainv = torch.linalg.inv(A)
+
+    def grad_of(v):                         # v (..., Nn, 2) -> G (..., Nn, 2, 2), G[c][i] = d v_c / d x_i
+        dv = v[..., nid, :] - v[..., :, None, :]
+        Bm = torch.einsum("nk,nki,...nkc->...nic", w, dX, dv)
+        return torch.einsum("nij,...njc->...nci", Ainv, Bm)
+
+    G = grad_of(u)
+    F = torch.eye(2, dtype=torch.float64, device=dev) + G
+    dG = grad_of(du.to(torch.float64))
+    dE = 0.5 * (dG.transpose(-1, -2) @ F + F.transpose(-1, -2) @ dG)
+    return torch.stack([dE[..., 0, 0], dE[..., 1, 1], 0.5 * (dE[..., 0, 1] + dE[..., 1, 0])], dim=-1)
+
+
+class _DICSolveFn(torch.autograd.Function):
+    """u* = solve(I2) with the implicit adjoint as backward and jvp."""
+
+    @staticmethod
+    def forward(image, holder):
+        return holder.forward_solve(image)
+
+    @staticmethod
+    def setup_context(ctx, inputs, output):
+        ctx.holder = inputs[1]
+
+    @staticmethod
+    def backward(ctx, grad_u):
+        return ctx.holder.adj.vjp(grad_u[None])[0].to(grad_u.dtype), None
+
+    @staticmethod
+    def jvp(ctx, d_image, _):
+        return ctx.holder.adj.jvp(d_image[None])[0].to(torch.float32)
+
+
+class DifferentiableSolve:
+    """``u = ds(image)``: the converged solve as a differentiable torch function of the deformed image.
+
+    Forward: the CG engine (the solver's MeshDICConfig) from ``u0``, then
+    ``polish`` exact Newton steps; the adjoint is linearised at that point.
+    """
+
+    def __init__(self, solver, state, u0=None, polish: int = 3, exact: bool = True):
+        self.solver, self.state = solver, state
+        self.u0 = u0
+        self.polish = int(polish)
+        self.exact = exact
+        self.adj = None
+
+    def forward_solve(self, image):
+        st = self.state
+        st.u0_nodal = None if self.u0 is None else np.asarray(self.u0, dtype=np.float32)
+        img = image.detach().to(torch.float32)
+        res = self.solver.solve(st, img)
+        u = torch.as_tensor(res.u_nodal, device=img.device)
+        if self.polish:
+            u = newton_polish(self.solver, st, img, u, st.config.reg_strength, self.polish, self.exact)
+        slot = self.solver._ensure(st)
+        slot.load_image(img)
+        self.adj = ImplicitAdjoint(slot, u, st.config.reg_strength, self.exact)
+        return u.clone()
+
+    def __call__(self, image: torch.Tensor) -> torch.Tensor:
+        return _DICSolveFn.apply(image, self)

@@ -196,6 +196,34 @@ D2IC_API int d2ic_cg_solve_noalloc(const d2ic_frame_t *frame, int interp_kind, v
 D2IC_API int d2ic_eval_objective(const d2ic_frame_t *frame, const float *u, void *control, size_t control_bytes,
                         int interp_kind, double *J_out, float *grad_out, void *stream);
 
+/* ---- implicit derivative of the converged solve (the hand-written replacement
+ *      for jax.jvp through _cg_solve in doc/11_Advanced_Use_Uncertainty_Propagation.ipynb,
+ *      cells 14/22/30).  frame_dev: the solved frame's descriptor (device); u: the
+ *      converged displacement (2*n_nodes).  Vectors of K right-hand sides are laid
+ *      out (node, component, k) with k fastest. ---- */
+
+/* Per chunk, the 10 distinct 2x2 blocks (xx, xy, yy) of sum_p N_a N_b M_p with
+ * M_p = grad I2 grad I2^T (+ r hess I2 when exact): 32 floats per chunk. */
+D2IC_API int d2ic_hessian_chunks(const d2ic_frame_t *frame_dev, int n_chunks, const float *u, int exact,
+                                 float *chunk_hess, void *stream);
+/* Y = H V for K vectors: chunk blocks / Np + alpha_reg * spring Hessian.  slots:
+ * node_chunk_k * n_nodes * 2 * K floats of scratch. */
+D2IC_API int d2ic_hessian_matvec(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, const float *chunk_hess,
+                                 const float *V, int K, float inv_np, float alpha_reg, float *slots, float *Y,
+                                 void *stream);
+/* Column k of out (n_nodes x 2 x K) = scale * (d grad_u J / dI2) dI, dI given by its
+ * B-spline coefficients (halo layout of the frame).  slots: node_chunk_k * n_nodes * 2 floats. */
+D2IC_API int d2ic_mixed_term(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, const float *u,
+                             const float *dcoeff, float scale, float *slots, float *out, int K, int k, void *stream);
+/* Adjoint of d2ic_mixed_term: gcoeff (halo layout, zeroed by the caller) += scale *
+ * (d grad_u J / dI2 coefficients)^T lambda, by atomic scatter (backward of the bicubic sampling). */
+D2IC_API int d2ic_mixed_term_T(const d2ic_frame_t *frame_dev, int n_chunks, const float *u, const float *lam,
+                               float scale, float *gcoeff, void *stream);
+/* Transpose of d2ic_bspline_prefilter: image-space gradient from a coefficient-space one.
+ * tmp: H x cpitch floats. */
+D2IC_API int d2ic_bspline_prefilter_T(const float *gcoeff, int H, int W, int pad, int cpitch, float *tmp, float *gimg,
+                                      void *stream);
+
 /* ---- initial motion (replaces _match_centers_jax, d2ic/solver_translation_zncc.py:118-168,
  *      and _project_centers_to_nodes_idw, d2ic/dic_init_motion.py:64-91) ---- */
 D2IC_API int d2ic_zncc_match(const float *ref, int Hr, int Wr, const float *def, int Hd, int Wd,

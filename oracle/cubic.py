@@ -106,6 +106,42 @@ def cubic_sample(coeff: np.ndarray, pad: int, x, y, with_grad: bool = False):
     return val
 
 
+def bspline_weights2(t):
+    """Second derivatives of the cubic B-spline weights for taps -1, 0, 1, 2."""
+    return np.stack([1.0 - t, 3.0 * t - 2.0, -3.0 * t + 1.0, t])
+
+
+def cubic_sample_hessian(coeff: np.ndarray, pad: int, x, y):
+    """Value, gradient and Hessian (d2/dx2, d2/dxdy, d2/dy2) of the spline at (x, y)."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    Hc, Wc = coeff.shape
+    ix = np.floor(x).astype(np.int64)
+    iy = np.floor(y).astype(np.int64)
+    tx, ty = x - ix, y - iy
+    wx, dwx = bspline_weights(tx)
+    wy, dwy = bspline_weights(ty)
+    ddwx, ddwy = bspline_weights2(tx), bspline_weights2(ty)
+    out = {k: np.zeros_like(x) for k in ("v", "gx", "gy", "hxx", "hxy", "hyy")}
+    for a in range(4):
+        rr = np.clip(iy - 1 + a + pad, 0, Hc - 1)
+        rv = np.zeros_like(x)
+        rd = np.zeros_like(x)
+        rdd = np.zeros_like(x)
+        for b in range(4):
+            cv = coeff[rr, np.clip(ix - 1 + b + pad, 0, Wc - 1)]
+            rv += wx[b] * cv
+            rd += dwx[b] * cv
+            rdd += ddwx[b] * cv
+        out["v"] += wy[a] * rv
+        out["gx"] += wy[a] * rd
+        out["gy"] += dwy[a] * rv
+        out["hxx"] += wy[a] * rdd
+        out["hxy"] += dwy[a] * rd
+        out["hyy"] += ddwy[a] * rv
+    return out
+
+
 def linear_sample(image: np.ndarray, x, y, with_grad: bool = False):
     """Bilinear sample at pixel-centre coordinates ``(x, y)`` (x = col + 0.5).
 
