@@ -83,6 +83,7 @@ class ImplicitAdjoint:
         if need > self._slots_cap:
             self._slots = torch.empty(need, dtype=torch.float32, device=self.dev)
             self._slots_cap = need
+        self._slots[:need].zero_()            # slots that no chunk owns must read as 0 (layout depends on K)
         Y = torch.empty_like(Vf)
         _lib.call("d2ic_hessian_matvec", ptr(self.desc), L.n_chunks, L.n_nodes, ptr(self.hess), ptr(Vf), K,
                   self.inv_np, self.alpha, ptr(self._slots), ptr(Y), _lib.stream_handle())
