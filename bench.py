@@ -215,8 +215,9 @@ def run_reference(args, ws, rank):
             "config": {"workload": wl.name, "frames": args.frames},
             "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference is JAX; jax/im_jax cannot be installed offline, so this arm times the "
-                    "project's FP64 C restatement of its CG solve on the host cores"}
+            "note": "the reference is JAX: its offline install fails on dm-pix and, with --no-deps, it does "
+                    "not import (no jax), so this arm times the project's FP64 C restatement of its CG "
+                    "solve on the host cores"}
     print(json.dumps(line), flush=True)
 
 

@@ -232,6 +232,10 @@ class DifferentiableSolve:
 
     Forward: the CG engine (the solver's MeshDICConfig) from ``u0``, then
     ``polish`` exact Newton steps; the adjoint is linearised at that point.
+    Reverse mode through ``backward()``, forward mode through
+    ``torch.autograd.forward_ad`` dual tensors.  ``torch.func`` transforms are
+    not supported: their wrapped tensors have no device pointer to hand to the
+    kernels.
     """
 
     def __init__(self, solver, state, u0=None, polish: int = 3, exact: bool = True):

@@ -88,9 +88,11 @@ def test_autograd_function_backward_and_jvp(problem):
     (u * w).sum().backward()
     ref = ds.adj.vjp(w[None].to(torch.float64))[0]
     assert torch.allclose(img.grad.to(torch.float64), ref.to(torch.float64), rtol=1e-4, atol=1e-9)
+    import torch.autograd.forward_ad as fwAD
     d = torch.ones_like(p["img"]) * 0.5
-    _, tangent = torch.func.jvp(lambda x: DifferentiableSolve(p["dic"].solver, p["dic"].state,
-                                                              u0=p["u"].cpu().numpy(), polish=2)(x), (p["img"],), (d,))
+    fw = DifferentiableSolve(p["dic"].solver, p["dic"].state, u0=p["u"].cpu().numpy(), polish=2)
+    with fwAD.dual_level():
+        tangent = fwAD.unpack_dual(fw(fwAD.make_dual(p["img"], d))).tangent
     direct = ds.adj.jvp(d[None])[0]
     assert torch.allclose(tangent.to(torch.float64), direct.to(torch.float64), rtol=1e-3, atol=1e-7)
 
