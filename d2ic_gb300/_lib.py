@@ -28,10 +28,11 @@ CMD_INIT, CMD_RUN, CMD_IDLE = 0, 1, 2
 
 INTERP_CUBIC = 0
 INTERP_LINEAR = 1
-NODE_GROUP = 512
-NPART = 6
+NODE_GROUP = 32
+NPART = 5
 MAX_FRAMES = 4096
 CHUNK_MAX = 256
+TILE_MAX_FLOATS = 736
 
 STATUS_NAMES = {OK: "ok", BAD_ARG: "bad_arg", OOM: "oom", NAN_DETECTED: "nan_detected",
                 MAX_ITERS: "max_iters", WAIT_TIMEOUT: "wait_timeout", CUDA_ERROR: "cuda_error",
@@ -47,21 +48,22 @@ szt = ctypes.c_size_t
 class Frame(ctypes.Structure):
     """Mirror of ``d2ic_frame_t``."""
     _fields_ = [
+        ("coeff_map", ctypes.c_uint64 * 16),
         ("coeff", vp), ("pix", vp), ("chunk_begin", vp), ("chunk_nodes", vp),
-        ("chunk_box", vp), ("chunk_slot", vp), ("nbr_index", vp), ("nbr_weight", vp),
+        ("chunk_box", vp), ("chunk_slot", vp), ("group_need", vp), ("nbr_index", vp), ("nbr_weight", vp),
         ("u0", vp), ("u_out", vp), ("hist", vp), ("n_iters", vp), ("status", vp), ("n_evals", vp),
-        ("node_ws", vp), ("chunk_J", vp), ("node_grad", vp), ("group_part", vp),
+        ("node_ws", vp), ("node_grad", vp), ("group_part", vp), ("group_cnt", vp), ("chunk_tile", vp),
         ("tol", f64), ("alpha_reg", f32), ("max_iter", i32),
         ("W", i32), ("H", i32), ("cpitch", i32), ("pad", i32),
         ("n_pix", i32), ("n_chunks", i32), ("n_nodes", i32), ("max_deg", i32),
-        ("n_groups", i32), ("chunks_per_group", i32),
-        ("node_chunk_k", i32), ("reserved_", i32),
+        ("n_groups", i32), ("node_chunk_k", i32), ("tile_w", i32), ("tile_h", i32), ("reserved_", i32 * 8),
     ]
 
 
 _SIGS = {
     "d2ic_last_error_string": (ctypes.c_char_p, []),
     "d2ic_version": (i32, []),
+    "d2ic_frame_descriptor_bytes": (szt, []),
     "d2ic_device_info": (i32, [i32, vp, vp]),
     "d2ic_bspline_prefilter": (i32, [vp, i32, i32, i32, i32, vp, vp, vp]),
     "d2ic_pad_image": (i32, [vp, i32, i32, i32, i32, vp, vp]),
@@ -69,6 +71,7 @@ _SIGS = {
     "d2ic_pack_pixels": (i32, [vp, vp, i32, vp, i32, i32, i32, i32, i32, vp, vp]),
     "d2ic_frame_workspace_bytes": (szt, [i32, i32, i32]),
     "d2ic_frame_bind_workspace": (i32, [vp, vp]),
+    "d2ic_frame_encode_tiles": (i32, [vp, i32, i32]),
     "d2ic_cg_control_bytes": (szt, [i32]),
     "d2ic_cg_solve_batched": (i32, [vp, i32, vp, szt, i32, i32, vp]),
     "d2ic_cg_solve_traced": (i32, [vp, i32, vp, szt, i32, i32, vp, i32, vp]),

@@ -25,4 +25,6 @@ int cuda_status(cudaError_t e, const char *what) {
 
 extern "C" const char *d2ic_last_error_string(void) { return d2ic::g_err; }
 
-extern "C" int d2ic_version(void) { return 100; }
+extern "C" int d2ic_version(void) { return 101; }
+
+extern "C" size_t d2ic_frame_descriptor_bytes(void) { return sizeof(d2ic_frame_t); }

@@ -34,24 +34,20 @@
 // Grid barriers are the engine's own (atomic counter + generation word) with a
 // globaltimer-bounded wait: a block that waits longer than D2IC_WAIT_NS sets
 // an abort flag and every block leaves the kernel at its next barrier.
+#include <cuda.h>   // CUtensorMap and its enums (the encoder is fetched from the driver at run time)
+#include <stddef.h>
+#include <string.h>
+
 #include "common.cuh"
 
 namespace d2ic {
 
-constexpr int NG = D2IC_NODE_GROUP;            // threads per block == nodes per group
-constexpr int NWARP = NG / 32;
+constexpr int NT = 512;                        // threads per block
+constexpr int NWARP = NT / 32;
+constexpr int GN = D2IC_NODE_GROUP;            // nodes per group: one per lane of the warp that reduces it
+static_assert(GN == 32, "a node group is one warp");
 #ifndef D2IC_ENGINE_MINB
 #define D2IC_ENGINE_MINB 1   // resident blocks per SM the register budget is sized for
-#endif
-// Staging each chunk's coefficient tile in shared memory measured slower than
-// reading the taps through L1 (each coefficient is reused by ~16 pixels of the
-// chunk, which L1 captures; the tile fill adds a dependent round trip per
-// chunk), so it is compiled out by default.
-#ifndef D2IC_ENGINE_TILE
-#define D2IC_ENGINE_TILE 0
-#endif
-#ifndef D2IC_ENGINE_RPL
-#define D2IC_ENGINE_RPL 8    // pixel records per lane prefetched at chunk start (<= 256 / 32)
 #endif
 constexpr unsigned long long WAIT_NS = 5ull * 1000ull * 1000ull * 1000ull;
 
@@ -80,7 +76,7 @@ struct CtlHeader {
     int total_chunks;
     int total_groups;
     int rounds;
-    unsigned work;
+    int finished;   // a frame finished in this round: the active list is rebuilt at the barrier
     int max_rounds;
     int pad_[6];
 };
@@ -158,41 +154,66 @@ __device__ __forceinline__ float2 *nbuf(const d2ic_frame_t &F, int j) {
 // Candidate point of the current round: u (EVAL) or u + alpha * dir with
 // dir = -g (restart / first iteration) or -g + beta * d_prev.  Explicit
 // round-to-nearest operations so that the P and N phases produce identical bits.
+// mode 0: u, 1: conjugate direction, 2: steepest descent.
+__device__ __forceinline__ float2 cand_value(float2 un, float2 gn, float2 dn, float alpha, float beta, int mode,
+                                             float2 &dir) {
+    if (mode == 0) {
+        dir = make_float2(0.f, 0.f);
+        return un;
+    }
+    float dx = -gn.x, dy = -gn.y;
+    if (mode == 1) {
+        dx = __fadd_rn(dx, __fmul_rn(beta, dn.x));
+        dy = __fadd_rn(dy, __fmul_rn(beta, dn.y));
+    }
+    dir = make_float2(dx, dy);
+    return make_float2(__fadd_rn(un.x, __fmul_rn(alpha, dx)), __fadd_rn(un.y, __fmul_rn(alpha, dy)));
+}
+
+// The candidate rule of a frame for the current round, read from its state
+// with L2 loads (not volatile) so that the reads are in flight together.
+struct FInfo {
+    float alpha, beta;
+    int mode, iu, igc, idp, igt;
+};
+__device__ __forceinline__ FInfo frame_info(const FrameState *S) {
+    FInfo fi;
+    fi.iu = __ldcg(&S->iu);
+    fi.igc = __ldcg(&S->igc);
+    fi.idp = __ldcg(&S->idp);
+    fi.igt = __ldcg(&S->igt);
+    const int st = __ldcg(&S->state), k = __ldcg(&S->k), rs = __ldcg(&S->restart);
+    fi.alpha = __ldcg(&S->alpha);
+    fi.beta = __ldcg(&S->beta);
+    fi.mode = (st == ST_EVAL) ? 0 : ((rs || k == 0) ? 2 : 1);
+    return fi;
+}
+
 struct Cand {
     const float2 *u, *g, *d;
     float alpha, beta;
-    int mode;   // 0: u, 1: conjugate direction, 2: steepest descent
+    int mode;
     __device__ __forceinline__ float2 at(int n, float2 &dir) const {
         const float2 un = __ldcg(u + n);
-        if (mode == 0) {
-            dir = make_float2(0.f, 0.f);
-            return un;
-        }
-        const float2 gn = __ldcg(g + n);
-        float dx = -gn.x, dy = -gn.y;
-        if (mode == 1) {
-            const float2 dn = __ldcg(d + n);
-            dx = __fadd_rn(dx, __fmul_rn(beta, dn.x));
-            dy = __fadd_rn(dy, __fmul_rn(beta, dn.y));
-        }
-        dir = make_float2(dx, dy);
-        return make_float2(__fadd_rn(un.x, __fmul_rn(alpha, dx)), __fadd_rn(un.y, __fmul_rn(alpha, dy)));
+        const float2 gn = mode != 0 ? __ldcg(g + n) : make_float2(0.f, 0.f);
+        const float2 dn = mode == 1 ? __ldcg(d + n) : make_float2(0.f, 0.f);
+        return cand_value(un, gn, dn, alpha, beta, mode, dir);
     }
 };
 
-__device__ __forceinline__ Cand make_cand(const d2ic_frame_t &F, const FrameState *S) {
+__device__ __forceinline__ Cand make_cand(const d2ic_frame_t &F, const FInfo &fi) {
     Cand c;
-    // L2 loads (not volatile) so that the eight reads are in flight together
-    const int iu = __ldcg(&S->iu), igc = __ldcg(&S->igc), idp = __ldcg(&S->idp);
-    const int st = __ldcg(&S->state);
-    c.u = nbuf(F, iu);
-    c.g = nbuf(F, 2 + igc);
-    c.d = nbuf(F, 5 + idp);
-    c.alpha = __ldcg(&S->alpha);
-    c.beta = __ldcg(&S->beta);
-    const int k = __ldcg(&S->k), rs = __ldcg(&S->restart);
-    c.mode = (st == ST_EVAL) ? 0 : ((rs || k == 0) ? 2 : 1);
+    c.u = nbuf(F, fi.iu);
+    c.g = nbuf(F, 2 + fi.igc);
+    c.d = nbuf(F, 5 + fi.idp);
+    c.alpha = fi.alpha;
+    c.beta = fi.beta;
+    c.mode = fi.mode;
     return c;
+}
+
+__device__ __forceinline__ Cand make_cand(const d2ic_frame_t &F, const FrameState *S) {
+    return make_cand(F, frame_info(S));
 }
 
 // ---------------------------------------------------------------------------
@@ -249,36 +270,143 @@ __device__ __forceinline__ int find_slot(const int *pre, int n, int x) {
 }
 
 // ---------------------------------------------------------------------------
-// P phase: one chunk per warp
+// P phase: one chunk per warp, software-pipelined
 // ---------------------------------------------------------------------------
-constexpr int RPL = D2IC_ENGINE_RPL;          // pixel records per lane, prefetched together
-constexpr int TILE_CAP = 1024;                // floats of the per-warp coefficient tile
+// Each warp walks its chunks (c, c + W, c + 2W, ... for W warps in the grid)
+// with three stages in flight:
+//   chunk i + 2: metadata (pixel range, nodes, slots) loaded into registers;
+//   chunk i + 1: pixel records copied into the warp's shared-memory buffer by
+//                one TMA bulk copy (cp.async.bulk, completion on an mbarrier),
+//                nodal candidate inputs (u, g, d) loaded into registers;
+//   chunk i:     sampled and reduced.
+// A warp therefore never waits on a metadata -> records / candidates round
+// trip; only the coefficient taps are read on demand (L1 captures their reuse).
+// Each chunk also stages its window of the deformed image's coefficients
+// (tile_w x tile_h floats) with a 2-D TMA copy on the same mbarrier.  The
+// window is placed from the chunk's candidate of the previous pass, with a
+// margin of TILE_MARGIN pixels on every side (stored per chunk in
+// chunk_tile); a pixel whose 4x4 stencil is not inside it (a larger move, the
+// first pass) reads global memory with the same arithmetic.
+constexpr int CHUNK_BYTES = D2IC_CHUNK_MAX * 16;            // one staged record buffer
+constexpr int TILE_BYTES = D2IC_TILE_MAX_FLOATS * 4;        // one staged coefficient tile
+static_assert(TILE_BYTES % 128 == 0, "tile buffers keep 128-byte alignment");
+constexpr int WARP_SMEM = 2 * CHUNK_BYTES + 2 * TILE_BYTES;
+constexpr int TILE_MARGIN = 2;
+constexpr int TILE_NONE = (int)0x80008000u;                 // no valid origin (col = row = -32768)
+constexpr unsigned long long TMA_WAIT_NS = 200ull * 1000ull * 1000ull;
+constexpr int FCACHE = 64;    // active frames whose per-round lookup data is kept in shared memory
 
-// Since the Q4 weights of a pixel inside its element are a convex combination,
-// every displaced pixel of a chunk lies in the chunk's pixel box shifted by
-// [min_a u_a, max_a u_a]; that box plus the cubic stencil and one pixel of
-// margin is staged in shared memory once per chunk.  A chunk whose tile would
-// not fit, or a pixel that lands outside it, reads global memory instead; both
-// paths feed the same tap arithmetic.
-template <int KIND>
-__device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &cd, int c, int lane, float *tile) {
-    const int pb = __ldg(F.chunk_begin + c), pe = __ldg(F.chunk_begin + c + 1);
-    const int2 box = __ldg(reinterpret_cast<const int2 *>(F.chunk_box) + c);
-    const uint4 *pix = reinterpret_cast<const uint4 *>(F.pix);
-    uint4 rec[RPL > 0 ? RPL : 1];
-#pragma unroll
-    for (int i = 0; i < RPL; ++i) {
-        const int p = pb + lane + 32 * i;
-        rec[i] = (p < pe) ? __ldg(pix + p) : make_uint4(0u, 0u, 0u, 0u);
-    }
-    float2 uc = make_float2(0.f, 0.f);
-    int nd = 0, slot = 0;
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(unsigned long long *b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+// 1-D TMA: global -> this CTA's shared memory, completion counted on mbarrier b
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, unsigned long long *b) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(b))
+                 : "memory");
+}
+// 2-D TMA: the tensor map's box at tensor coordinates (x, y) -> shared memory
+__device__ __forceinline__ void tensor_load_2d(void *dst, const void *map, int x, int y, unsigned long long *b) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_addr(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(smem_addr(b))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// false if the phase did not complete within TMA_WAIT_NS
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity) {
+    if (mbar_test(b, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    while (!mbar_test(b, parity))
+        if (gtimer() - t0 > TMA_WAIT_NS) return false;
+    return true;
+}
+
+// One chunk's metadata as the pipeline carries it.  nd / slot hold local node
+// (lane) a's index and slot rank in lanes 0..3.
+struct ChunkMeta {
+    int s, f, c, pb, pe, nd, slot;   // active slot, frame, chunk within the frame, ...
+    int box0, tile;                  // packed pixel-box corner and tile origin (col | row << 16)
+};
+
+__device__ __forceinline__ ChunkMeta load_meta(const d2ic_frame_t *frames, int f, int c, int lane) {
+    const d2ic_frame_t &F = frames[f];
+    ChunkMeta m;
+    m.s = 0;
+    m.f = f;
+    m.c = c;
+    m.pb = __ldg(F.chunk_begin + c);
+    m.pe = __ldg(F.chunk_begin + c + 1);
+    m.box0 = __ldg(F.chunk_box + 2 * c);
+    m.tile = F.tile_w > 0 ? __ldcg(F.chunk_tile + c) : TILE_NONE;   // rewritten every pass: L2
+    m.nd = 0;
+    m.slot = 0;
     if (lane < 4) {
-        nd = __ldg(F.chunk_nodes + 4 * c + lane);
-        slot = (int)(((unsigned)__ldg(F.chunk_slot + c) >> (8 * lane)) & 0xffu);
-        float2 dir;
-        uc = cd.at(nd, dir);
+        m.nd = __ldg(F.chunk_nodes + 4 * c + lane);
+        m.slot = (int)(((unsigned)__ldg(F.chunk_slot + c) >> (8 * lane)) & 0xffu);
     }
+    return m;
+}
+
+// raw candidate inputs of a chunk's nodes (lanes 0..3), combined when the chunk is processed
+struct CandRaw {
+    float2 u, g, d;
+};
+
+// Where a chunk's records and coefficient tile come from in this pass.
+struct Stage {
+    bool staged, tiled;   // records in shared memory; coefficient tile in shared memory
+    int tx0, ty0;         // tile origin (pixel column / row of tile element (0, 0))
+};
+
+// Tile origin for the next pass from this pass's nodal candidates: the
+// smallest tap column / row any pixel of the chunk can reach, less the margin.
+__device__ __forceinline__ int tile_origin(int box0, const float ux[4], const float uy[4]) {
+    const float mnx = fminf(fminf(ux[0], ux[1]), fminf(ux[2], ux[3]));
+    const float mny = fminf(fminf(uy[0], uy[1]), fminf(uy[2], uy[3]));
+    const int ox = (box0 & 0xffff) + (int)safe_floor(mnx) - 1 - TILE_MARGIN;
+    const int oy = (int)((unsigned)box0 >> 16) + (int)safe_floor(mny) - 1 - TILE_MARGIN;
+    if (ox <= -32768 || ox >= 32768 || oy <= -32768 || oy >= 32768) return TILE_NONE;   // also NaN candidates
+    return (ox & 0xffff) | (int)((unsigned)oy << 16);
+}
+
+// Release increment of a completion counter: the calling thread's earlier writes, and those of
+// the lanes it synchronised with (__syncwarp), are visible before the count.
+__device__ __forceinline__ void red_release_add(int *p, int v) {
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int atom_acq_rel_add(int *p, int v) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// `sig` (lanes 0..3): the group counter the previous chunk of this warp still has to count
+// (deferred so that its slot stores are long complete when the release is issued); on
+// return, this chunk's.
+template <int KIND>
+__device__ __forceinline__ void chunk_compute(const d2ic_frame_t &F, const ChunkMeta &m, float2 uc, const Stage &st,
+                                              const uint4 *srec, const float *tile, int lane, int *&sig) {
+    const bool staged = st.staged;
+    const bool tiled = KIND == D2IC_INTERP_CUBIC && st.tiled;
+    const int tw = F.tile_w, th = F.tile_h, tx0 = st.tx0, ty0 = st.ty0;
+    const int n = max(m.pe - m.pb, 0);
+    const uint4 *gpix = reinterpret_cast<const uint4 *>(F.pix) + m.pb;
     float ux[4], uy[4];
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -286,32 +414,6 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
         uy[a] = __shfl_sync(0xffffffffu, uc.y, a);
     }
     const Img im{F.coeff, F.W, F.H, F.cpitch, F.pad};
-    int tx0 = 0, ty0 = 0, tw = 0, th = 0;
-    bool use_tile = false;
-    if (KIND == D2IC_INTERP_CUBIC) {
-        const float mnx = fminf(fminf(ux[0], ux[1]), fminf(ux[2], ux[3]));
-        const float mxx = fmaxf(fmaxf(ux[0], ux[1]), fmaxf(ux[2], ux[3]));
-        const float mny = fminf(fminf(uy[0], uy[1]), fminf(uy[2], uy[3]));
-        const float mxy = fmaxf(fmaxf(uy[0], uy[1]), fmaxf(uy[2], uy[3]));
-        const int bx0 = box.x & 0xffff, by0 = (int)((unsigned)box.x >> 16);
-        const int bx1 = box.y & 0xffff, by1 = (int)((unsigned)box.y >> 16);
-        tx0 = bx0 + (int)safe_floor(mnx) - 2;
-        ty0 = by0 + (int)safe_floor(mny) - 2;
-        tw = bx1 + (int)safe_floor(mxx) + 3 - tx0 + 1;
-        th = by1 + (int)safe_floor(mxy) + 3 - ty0 + 1;
-        use_tile = D2IC_ENGINE_TILE && tw >= 4 && th >= 4 && tw <= 64 && tw * th <= TILE_CAP;
-        if (use_tile) {
-            // one tile row per warp instruction: lane -> column (two columns per lane when tw > 32)
-            const int c0 = clampi(tx0 + lane, -im.pad, im.W - 1 + im.pad) + im.pad;
-            const int c1 = clampi(tx0 + lane + 32, -im.pad, im.W - 1 + im.pad) + im.pad;
-            for (int ly = 0; ly < th; ++ly) {
-                const float *row = im.c + (size_t)(clampi(ty0 + ly, -im.pad, im.H - 1 + im.pad) + im.pad) * im.cp;
-                if (lane < tw) tile[ly * tw + lane] = __ldg(row + c0);
-                if (lane + 32 < tw) tile[ly * tw + lane + 32] = __ldg(row + c1);
-            }
-            __syncwarp();
-        }
-    }
     float jr = 0.f;
     float gxa[4] = {0.f, 0.f, 0.f, 0.f}, gya[4] = {0.f, 0.f, 0.f, 0.f};
     auto one = [&](const uint4 r4) {
@@ -327,8 +429,8 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
         split_coord(x, dx, ix, tx);
         split_coord(y, dy, iy, ty);
         float gx, gy, v;
-        const int lx = ix - 1 - tx0, ly = iy - 1 - ty0;
-        if (use_tile && lx >= 0 && ly >= 0 && lx <= tw - 4 && ly <= th - 4)
+        const int lx = ix - 1 - tx0, ly = iy - 1 - ty0;   // stencil corner inside the tile
+        if (tiled && (unsigned)lx <= (unsigned)(tw - 4) && (unsigned)ly <= (unsigned)(th - 4))
             v = sample_cubic_tile(tile, tw, lx, ly, tx, ty, gx, gy);
         else
             v = sample<KIND>(im, ix, iy, tx, ty, gx, gy);
@@ -341,125 +443,122 @@ __device__ __forceinline__ void pixel_chunk(const d2ic_frame_t &F, const Cand &c
             gya[a] += rgy * N[a];
         }
     };
-#pragma unroll
-    for (int i = 0; i < RPL; ++i)
-        if (pb + lane + 32 * i < pe) one(rec[i]);
-    for (int p = pb + lane + 32 * RPL; p < pe; p += 32) one(__ldg(pix + p));   // chunks longer than the prefetch
+    if (staged) {
+#pragma unroll 4
+        for (int i = 0; i < D2IC_CHUNK_MAX / 32; ++i) {
+            const int p = lane + 32 * i;
+            if (p < n) one(srec[p]);
+        }
+        for (int p = lane + D2IC_CHUNK_MAX; p < n; p += 32) one(__ldg(gpix + p));   // beyond the staged buffer
+    } else {
+        for (int p = lane; p < n; p += 32) one(__ldg(gpix + p));
+    }
     const DF js = df_warp_sum(DF{jr, 0.f});
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
         gxa[a] = warp_sum_f(gxa[a]);
         gya[a] = warp_sum_f(gya[a]);
     }
-    if (lane == 0) reinterpret_cast<float2 *>(F.chunk_J)[c] = make_float2(js.hi, js.lo);   // double-float
-    if (lane < 4) {                                 // lane a stores node a's partial in the chunk's slot
+    if (lane == 0 && tw > 0) F.chunk_tile[m.c] = tile_origin(m.box0, ux, uy);
+    if (sig) red_release_add(sig, 1);              // the previous chunk's counts (its slots are old)
+    // lane a stores node a's partial in the chunk's slot of that node; node 0's slot also
+    // carries the chunk's sum of r^2 (double-float), so every chunk is counted exactly once
+    if (lane < 4) {
         const float gx = lane == 0 ? gxa[0] : lane == 1 ? gxa[1] : lane == 2 ? gxa[2] : gxa[3];
         const float gy = lane == 0 ? gya[0] : lane == 1 ? gya[1] : lane == 2 ? gya[2] : gya[3];
-        reinterpret_cast<float2 *>(F.node_grad)[(size_t)slot * F.n_nodes + nd] = make_float2(gx, gy);
+        reinterpret_cast<float4 *>(F.node_grad)[(size_t)m.slot * F.n_nodes + m.nd] =
+            make_float4(gx, gy, lane == 0 ? js.hi : 0.f, lane == 0 ? js.lo : 0.f);
     }
-    __syncwarp();                                   // the tile is reused by the warp's next chunk
+    // one count per distinct node group of the chunk (the group's reducer waits for all of them),
+    // issued by the lane holding the group's first node after the next chunk or the pixel pass ends
+    const int grp = m.nd / GN;
+    const int g0 = __shfl_sync(0xffffffffu, grp, 0), g1 = __shfl_sync(0xffffffffu, grp, 1),
+              g2 = __shfl_sync(0xffffffffu, grp, 2);
+    const bool first = lane == 0 || (lane == 1 && grp != g0) || (lane == 2 && grp != g0 && grp != g1) ||
+                       (lane == 3 && grp != g0 && grp != g1 && grp != g2);
+    sig = (lane < 4 && first) ? F.group_cnt + grp : nullptr;
+    __syncwarp();                                   // every lane is done with the staged buffers
 }
 
 // ---------------------------------------------------------------------------
-// N phase: one group of NG nodes per block
+// N work: one group of GN = 32 nodes per warp (lane = node)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void node_group(const d2ic_frame_t &F, const FrameState *S, int g, DF (*red)[NWARP]) {
-    const Cand cd = make_cand(F, S);
-    const int n = g * NG + threadIdx.x;
-    const int igt = __ldcg(&S->igt), igc = __ldcg(&S->igc), iu = __ldcg(&S->iu), idp = __ldcg(&S->idp);
-    DF q[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    if (n < F.n_nodes) {
-        // All loads of a batch are issued before any is consumed: the node pass
-        // is a short chain of L2 round trips instead of one per table entry.
-        // Sums still run in table order.
-        constexpr int NB = 4;
-        const float2 gc = __ldcg(nbuf(F, 2 + igc) + n);  // issued with the candidate's own loads
-        float2 dir;
-        const float2 ui = cd.at(n, dir);
-        // chunk partials from the node's K slots (unused slots hold 0), in slot order
-        float sx = 0.f, sy = 0.f;
-        const int K = F.node_chunk_k, Nn = F.n_nodes;
-        const float2 *ng = reinterpret_cast<const float2 *>(F.node_grad) + n;
-        for (int kb = 0; kb < K; kb += NB) {
-            float2 v[NB];
+// Per node: gather its chunk partials from its K slots (slot order), add the
+// spring gradient over the neighbour table, write the trial gradient, trial
+// point and trial direction, and return the node's terms of sum r^2 (from the
+// slots), spring energy, g.g, g.(g - g_cur) and g_cur.dir in double-float.
+__device__ __forceinline__ void node_work(const d2ic_frame_t &F, const FInfo &fi, int g, int lane, DF q[5]) {
 #pragma unroll
-            for (int q = 0; q < NB; ++q) v[q] = (kb + q < K) ? __ldcg(ng + (size_t)(kb + q) * Nn) : make_float2(0.f, 0.f);
+    for (int i = 0; i < 5; ++i) q[i] = DF{0.f, 0.f};
+    const int n = g * GN + lane;
+    if (n >= F.n_nodes) return;
+    const Cand cd = make_cand(F, fi);
+    // All loads of a batch are issued before any is consumed: the node pass is a short
+    // chain of L2 round trips instead of one per table entry.  Sums still run in table order.
+    const float2 gc = __ldcg(nbuf(F, 2 + fi.igc) + n);   // issued with the candidate's own loads
+    float2 dir;
+    const float2 ui = cd.at(n, dir);
+    float sx = 0.f, sy = 0.f;
+    DF sj = {0.f, 0.f};
+    const int K = F.node_chunk_k, Nn = F.n_nodes;
+    const float4 *ng = reinterpret_cast<const float4 *>(F.node_grad) + n;
+    constexpr int NB = 4;
+    for (int kb = 0; kb < K; kb += NB) {
+        float4 v[NB];
 #pragma unroll
-            for (int q = 0; q < NB; ++q)
-                if (kb + q < K) {
-                    sx += v[q].x;
-                    sy += v[q].y;
-                }
-        }
-        float rx = 0.f, ry = 0.f, en = 0.f;
-        const int md = F.max_deg;
-        const int *nbi = F.nbr_index + n;             // column-major: entry k at k * n_nodes
-        const float *nbw = F.nbr_weight + n;
-        bool alive = true;                               // entries after the first -1 are padding
-        constexpr int NBN = 8;
-        for (int kb = 0; kb < md && alive; kb += NBN) {
-            int jj[NBN];
-            float ww[NBN];
+        for (int t = 0; t < NB; ++t) v[t] = (kb + t < K) ? __ldcg(ng + (size_t)(kb + t) * Nn) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-            for (int q = 0; q < NBN; ++q) {
-                jj[q] = (kb + q < md) ? __ldg(nbi + (size_t)(kb + q) * Nn) : -1;
-                ww[q] = (kb + q < md) ? __ldg(nbw + (size_t)(kb + q) * Nn) : 0.f;
+        for (int t = 0; t < NB; ++t)
+            if (kb + t < K) {
+                sx += v[t].x;
+                sy += v[t].y;
+                sj = df_add(sj, DF{v[t].z, v[t].w});
             }
-            float2 uj[NBN];
+    }
+    float rx = 0.f, ry = 0.f, en = 0.f;
+    const int md = F.max_deg;
+    const int *nbi = F.nbr_index + n;             // column-major: entry k at k * n_nodes
+    const float *nbw = F.nbr_weight + n;
+    bool alive = true;                               // entries after the first -1 are padding
+    constexpr int NBN = 8;
+    for (int kb = 0; kb < md && alive; kb += NBN) {
+        int jj[NBN];
+        float ww[NBN];
 #pragma unroll
-            for (int q = 0; q < NBN; ++q) {
-                float2 dj;
-                uj[q] = (jj[q] >= 0) ? cd.at(jj[q], dj) : make_float2(0.f, 0.f);
+        for (int t = 0; t < NBN; ++t) {
+            jj[t] = (kb + t < md) ? __ldg(nbi + (size_t)(kb + t) * Nn) : -1;
+            ww[t] = (kb + t < md) ? __ldg(nbw + (size_t)(kb + t) * Nn) : 0.f;
+        }
+        float2 uj[NBN];
+#pragma unroll
+        for (int t = 0; t < NBN; ++t) {
+            float2 dj;
+            uj[t] = (jj[t] >= 0) ? cd.at(jj[t], dj) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int t = 0; t < NBN; ++t) {
+            alive = alive && jj[t] >= 0;
+            if (alive) {
+                const float ddx = ui.x - uj[t].x, ddy = ui.y - uj[t].y;
+                rx += ww[t] * ddx;
+                ry += ww[t] * ddy;
+                en += ww[t] * (ddx * ddx + ddy * ddy);
             }
-#pragma unroll
-            for (int q = 0; q < NBN; ++q) {
-                alive = alive && jj[q] >= 0;
-                if (alive) {
-                    const float ddx = ui.x - uj[q].x, ddy = ui.y - uj[q].y;
-                    rx += ww[q] * ddx;
-                    ry += ww[q] * ddy;
-                    en += ww[q] * (ddx * ddx + ddy * ddy);
-                }
-            }
-        }
-        const float inv_np = 1.0f / (float)max(F.n_pix, 1);
-        const float gx = sx * inv_np + F.alpha_reg * rx;
-        const float gy = sy * inv_np + F.alpha_reg * ry;
-        nbuf(F, 2 + igt)[n] = make_float2(gx, gy);
-        nbuf(F, 1 - iu)[n] = ui;
-        nbuf(F, 5 + (1 - idp))[n] = dir;
-        // per-node terms of the inner products, exact in double-float (g - g_cur rounded
-        // in FP32 as the reference's elementwise difference)
-        q[P_EREG] = DF{0.25f * en, 0.f};
-        q[P_GG] = df_add(df_prod(gx, gx), df_prod(gy, gy));
-        q[P_GDIFF] = df_add(df_prod(gx, gx - gc.x), df_prod(gy, gy - gc.y));
-        q[P_GD] = df_add(df_prod(gc.x, dir.x), df_prod(gc.y, dir.y));
-    }
-    // this group's share of the chunk sums of r^2
-    {
-        const int c0 = g * F.chunks_per_group;
-        const int c1 = min(c0 + F.chunks_per_group, F.n_chunks);
-        const float2 *cj = reinterpret_cast<const float2 *>(F.chunk_J);
-        for (int c = c0 + (int)threadIdx.x; c < c1; c += NG) {
-            const float2 v = __ldcg(cj + c);
-            q[P_JSUM] = df_add(q[P_JSUM], DF{v.x, v.y});
         }
     }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        const DF v = df_warp_sum(q[i]);
-        if (lane == 0) red[i][wid] = v;
-    }
-    __syncthreads();
-    if (wid == 0) {                                // warp 0: one warp-sum per quantity, fixed order
-#pragma unroll
-        for (int i = 0; i < 5; ++i) {
-            const DF v = df_warp_sum(lane < NWARP ? red[i][lane] : DF{0.f, 0.f});
-            if (lane == 0) F.group_part[(size_t)g * D2IC_NPART + i] = df_to_double(v);
-        }
-    }
-    __syncthreads();
+    const float inv_np = 1.0f / (float)max(F.n_pix, 1);
+    const float gx = sx * inv_np + F.alpha_reg * rx;
+    const float gy = sy * inv_np + F.alpha_reg * ry;
+    nbuf(F, 2 + fi.igt)[n] = make_float2(gx, gy);
+    nbuf(F, 1 - fi.iu)[n] = ui;
+    nbuf(F, 5 + (1 - fi.idp))[n] = dir;
+    // per-node terms of the inner products, exact in double-float (g - g_cur rounded
+    // in FP32 as the reference's elementwise difference)
+    q[P_JSUM] = sj;
+    q[P_EREG] = DF{0.25f * en, 0.f};
+    q[P_GG] = df_add(df_prod(gx, gx), df_prod(gy, gy));
+    q[P_GDIFF] = df_add(df_prod(gx, gx - gc.x), df_prod(gy, gy - gc.y));
+    q[P_GD] = df_add(df_prod(gc.x, dir.x), df_prod(gc.y, dir.y));
 }
 
 // ---------------------------------------------------------------------------
@@ -588,7 +687,7 @@ __device__ __forceinline__ void block_scan3(int &a, int &b, int &c, int &ta, int
 
 // rebuild the active list and prefix sums (whole block)
 __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
-    const int per = (n_frames + NG - 1) / NG;
+    const int per = (n_frames + NT - 1) / NT;
     const int f0 = threadIdx.x * per, f1 = min(f0 + per, n_frames);
     int cnt = 0, ch = 0, gr = 0;
     for (int f = f0; f < f1; ++f)
@@ -624,7 +723,7 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
 // that finished in an earlier launch are marked reported (their outputs were
 // written at the end of that launch).
 __device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
-    for (int f = threadIdx.x; f < n_frames; f += NG) {
+    for (int f = threadIdx.x; f < n_frames; f += NT) {
         const int cmd = ld_vol(C.cmd + f);
         if (cmd == CMD_INIT) {
             FrameState S;
@@ -649,49 +748,67 @@ __device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
     rebuild_active(frames, n_frames, C);
 }
 
-__device__ void r_step(const d2ic_frame_t *frames, int n_frames, Ctl &C, int eval_only) {
-    __shared__ int s_finished;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_finished = 0;
-    __syncthreads();
-    const int na = ld_vol(&C.h->n_active);
-    for (int s = wid; s < na; s += NWARP) {
-        const int f = ld_vol(C.active + s);
-        const d2ic_frame_t &F = frames[f];
-        FrameState S;
-        if (lane == 0) S = load_fs(C.fs + f);          // issued together with the partial loads below
-        double q[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        for (int g = lane; g < F.n_groups; g += 32) {
+// The CG control of one frame, run by the warp that reduced the frame's last
+// node group: the group partials are summed in group order (double-float,
+// then FP64) and the frame state advanced.  Nothing else reads the frame's
+// state in this round once all its groups are reduced.
+__device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int lane) {
+    DF q[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    const int nsg = (F.n_groups + GN - 1) / GN;
+    const float2 *sp = reinterpret_cast<const float2 *>(F.group_part) + (size_t)F.n_groups * D2IC_NPART;
+    for (int g = lane; g < nsg; g += 32) {
+        float2 v[5];
 #pragma unroll
-            for (int i = 0; i < 5; ++i) q[i] += __ldcg(F.group_part + (size_t)g * D2IC_NPART + i);
-        }
+        for (int i = 0; i < 5; ++i) v[i] = __ldcg(sp + (size_t)g * D2IC_NPART + i);
 #pragma unroll
-        for (int i = 0; i < 5; ++i) q[i] = warp_sum_d(q[i]);
-        if (lane == 0) {
-            frame_decide(S, F, q, eval_only);
-            C.fs[f] = S;
-            if (S.state == ST_DONE) s_finished = 1;
-        }
+        for (int i = 0; i < 5; ++i) q[i] = df_add(q[i], DF{v[i].x, v[i].y});
     }
-    __syncthreads();
-    if (s_finished) rebuild_active(frames, n_frames, C);   // else the active lists stay as they are
+#pragma unroll
+    for (int i = 0; i < 5; ++i) q[i] = df_warp_sum(q[i]);
+    if (lane == 0) {
+        FrameState S = load_fs(C.fs + f);
+        double qd[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) qd[i] = df_to_double(q[i]);
+        frame_decide(S, F, qd, eval_only);
+        C.fs[f] = S;
+        if (S.state == ST_DONE) atomicExch(&C.h->finished, 1);
+    }
 }
 
 // ---------------------------------------------------------------------------
 // the persistent kernel
 // ---------------------------------------------------------------------------
 template <int KIND>
-__global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
+__global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
                                                    char *ctl_base, int eval_only, const float *u_eval,
                                                    double *J_out, float *grad_out, unsigned long long *trace,
                                                    int trace_rounds, int max_rounds) {
-    __shared__ DF red[5][NWARP];
-    extern __shared__ float s_tile[];              // NWARP * TILE_CAP floats
+    __shared__ unsigned long long s_bar[NWARP][2];   // per-warp mbarriers of the two record buffers
+    __shared__ int s_cpre[FCACHE + 1];               // per-round copies of the active list (na <= FCACHE)
+    __shared__ int s_gpre[FCACHE + 1];
+    __shared__ int s_act[FCACHE];
+    __shared__ FInfo s_fi[FCACHE];
+    // per warp: two record buffers, then two coefficient-tile buffers (all 128-byte aligned)
+    extern __shared__ __align__(128) unsigned char s_dyn[];
     Ctl C = make_ctl(ctl_base, n_frames);
-    const int lane = threadIdx.x & 31;
-    // optional phase trace: block 0 stamps [round start, after P barrier, end of its N, -, -, after R
-    // barrier, end of its own P work]; the last block stamps the start and end of its R step into
-    // slots 3 and 4
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned char *wbuf = s_dyn + (size_t)wid * WARP_SMEM;
+    unsigned pipe_i = 0;   // chunks this warp has staged: buffer i & 1, completion parity (i >> 1) & 1
+    if (lane == 0) {
+        mbar_init(&s_bar[wid][0], 1);
+        mbar_init(&s_bar[wid][1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // descriptors (and their tensor maps) may have been rewritten since the previous launch
+    for (int f = threadIdx.x; f < n_frames; f += NT)
+        if (frames[f].tile_w > 0)
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(frames[f].coeff_map) : "memory");
+    const bool tiles_ok = (smem_addr(s_dyn) & 127) == 0;   // tile buffers need 128-byte alignment
+    __syncthreads();
+    // optional phase trace per round: warp 0 of block 0 stamps [0] round start, [1] end of its pixel
+    // work, [2] end of its group work, [5] after the barrier; the warp that runs a frame's control
+    // stamps [3] and [4] around it
     const bool tr = trace != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
     int round = 0;
 
@@ -701,18 +818,33 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         const d2ic_frame_t &F = frames[f];
         const int nn = F.n_nodes;
         const float2 *u0 = reinterpret_cast<const float2 *>((eval_only && u_eval && f == 0) ? u_eval : F.u0);
-        for (int i = blockIdx.x * NG + threadIdx.x; i < nn; i += gridDim.x * NG) {
+        for (int i = blockIdx.x * NT + threadIdx.x; i < nn; i += gridDim.x * NT) {
             nbuf(F, 0)[i] = u0 ? u0[i] : make_float2(0.f, 0.f);
 #pragma unroll
             for (int j = 1; j < 7; ++j) nbuf(F, j)[i] = make_float2(0.f, 0.f);
         }
-        // gradient slots that no chunk owns must read as 0
-        float2 *ng = reinterpret_cast<float2 *>(F.node_grad);
-        for (size_t i = blockIdx.x * NG + threadIdx.x; i < (size_t)F.node_chunk_k * nn; i += (size_t)gridDim.x * NG)
-            ng[i] = make_float2(0.f, 0.f);
+        // gradient slots that no chunk owns must read as 0; group counters start at 0
+        float4 *ng = reinterpret_cast<float4 *>(F.node_grad);
+        for (size_t i = blockIdx.x * NT + threadIdx.x; i < (size_t)F.node_chunk_k * nn; i += (size_t)gridDim.x * NT)
+            ng[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int n_cnt = F.n_groups + (F.n_groups + GN - 1) / GN + 1;
+        for (int i = blockIdx.x * NT + threadIdx.x; i < n_cnt; i += gridDim.x * NT) F.group_cnt[i] = 0;
         if (F.hist)
-            for (int i = blockIdx.x * NG + threadIdx.x; i < 3 * F.max_iter; i += gridDim.x * NG)
+            for (int i = blockIdx.x * NT + threadIdx.x; i < 3 * F.max_iter; i += gridDim.x * NT)
                 F.hist[i] = __int_as_float(0x7fc00000);
+        // first-pass tile origins from u0 (the first pass evaluates u0 itself)
+        if (F.tile_w > 0)
+            for (int c = blockIdx.x * NT + threadIdx.x; c < F.n_chunks; c += gridDim.x * NT) {
+                float ux[4], uy[4];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const int nd = __ldg(F.chunk_nodes + 4 * c + a);
+                    const float2 v = u0 ? u0[nd] : make_float2(0.f, 0.f);
+                    ux[a] = v.x;
+                    uy[a] = v.y;
+                }
+                F.chunk_tile[c] = tile_origin(__ldg(F.chunk_box + 2 * c), ux, uy);
+            }
     }
     if (!grid_barrier(C.h, [&] { r_init(frames, n_frames, C); })) goto finish;
 
@@ -721,47 +853,209 @@ __global__ void __launch_bounds__(NG, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         if (na == 0) break;
         const bool trr = tr && round < trace_rounds;
         if (trr) trace[7 * round + 0] = gtimer();
-        // ---- P phase: chunk c of the active list goes to global warp c mod (warps in grid) ----
+        // ---- P phase: chunk g of the active list goes to global warp g mod (warps in grid) ----
         {
             const int total = ld_vol(&C.h->total_chunks);
-            const int gw = (int)((blockIdx.x * NG + threadIdx.x) >> 5);
-            const int nw = (int)((gridDim.x * NG) >> 5);
-            int cbase = 0, cend = 0;
-            const d2ic_frame_t *Fp = frames;
-            Cand cd;
-            for (int c = gw; c < total; c += nw) {
-                if (c >= cend) {                      // chunks ascend per warp: frames change forward only
-                    const int s = find_slot(C.cpre, na, c);
-                    const int f = __ldcg(C.active + s);
-                    cbase = __ldcg(C.cpre + s);
-                    cend = __ldcg(C.cpre + s + 1);
-                    Fp = frames + f;
-                    cd = make_cand(*Fp, C.fs + f);
+            const bool cached = na <= FCACHE;
+            if (cached) {
+                for (int s = threadIdx.x; s <= na; s += NT) {
+                    s_cpre[s] = __ldcg(C.cpre + s);
+                    s_gpre[s] = __ldcg(C.gpre + s);
                 }
-                pixel_chunk<KIND>(*Fp, cd, c - cbase, lane, s_tile + (threadIdx.x >> 5) * TILE_CAP);
+                for (int s = threadIdx.x; s < na; s += NT) {
+                    const int f = __ldcg(C.active + s);
+                    s_act[s] = f;
+                    s_fi[s] = frame_info(C.fs + f);
+                }
             }
-        }
-        if (trace != nullptr && blockIdx.x == 0 && round < trace_rounds) {
             __syncthreads();
-            if (threadIdx.x == 0) trace[7 * round + 6] = gtimer();
-        }
-        if (!grid_barrier(C.h, [] {})) break;
-        if (trr) trace[7 * round + 1] = gtimer();
-        // ---- N phase ----
-        {
-            const int tg = ld_vol(&C.h->total_groups);
-            for (int gi = blockIdx.x; gi < tg; gi += gridDim.x) {
-                const int s = find_slot(C.gpre, na, gi);
-                const int f = __ldcg(C.active + s);
-                node_group(frames[f], C.fs + f, gi - __ldcg(C.gpre + s), red);
+            const int gw = (int)((blockIdx.x * NT + threadIdx.x) >> 5);
+            const int nw = (int)((gridDim.x * NT) >> 5);
+            int cur = 0;   // active slot of the last located chunk (chunks ascend per warp)
+            auto fetch_meta = [&](int g) {
+                int s, f, base;
+                if (cached) {
+                    while (cur + 1 < na && s_cpre[cur + 1] <= g) ++cur;
+                    s = cur;
+                    f = s_act[s];
+                    base = s_cpre[s];
+                } else {
+                    s = find_slot(C.cpre, na, g);
+                    f = __ldcg(C.active + s);
+                    base = __ldcg(C.cpre + s);
+                }
+                ChunkMeta m = load_meta(frames, f, g - base, lane);
+                m.s = s;
+                return m;
+            };
+            // stage a chunk: TMA bulk copy of its records, 2-D TMA copy of its coefficient tile,
+            // loads of its nodal candidate inputs
+            auto issue = [&](const ChunkMeta &m, unsigned i, CandRaw &cr) {
+                const d2ic_frame_t &F = frames[m.f];
+                const int n = max(m.pe - m.pb, 0);
+                const unsigned bytes = (unsigned)min(n, D2IC_CHUNK_MAX) * 16u;
+                const uint4 *src = reinterpret_cast<const uint4 *>(F.pix) + m.pb;
+                Stage st;
+                st.staged = bytes > 0 && ((reinterpret_cast<uintptr_t>(src) & 15) == 0);
+                st.tiled = false;
+                st.tx0 = 0;
+                st.ty0 = 0;
+                if (KIND == D2IC_INTERP_CUBIC && tiles_ok && F.tile_w > 0 && m.tile != TILE_NONE) {
+                    st.tx0 = (int)(short)(m.tile & 0xffff) & ~3;   // TMA x: a multiple of 4 floats
+                    st.ty0 = (int)(short)((unsigned)m.tile >> 16);
+                    st.tiled = st.tx0 >= -F.pad && st.ty0 >= -F.pad && st.tx0 + F.tile_w <= F.W + F.pad &&
+                               st.ty0 + F.tile_h <= F.H + F.pad;   // inside the halo'd array: no fill
+                }
+                unsigned long long *bar = &s_bar[wid][i & 1];
+                if (lane == 0) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // after the buffers' generic reads
+                    const unsigned tbytes = st.tiled ? (unsigned)(F.tile_w * F.tile_h) * 4u : 0u;
+                    mbar_arrive_tx(bar, (st.staged ? bytes : 0u) + tbytes);
+                    if (st.staged) bulk_load(wbuf + (i & 1) * CHUNK_BYTES, src, bytes, bar);
+                    if (st.tiled)
+                        tensor_load_2d(wbuf + 2 * CHUNK_BYTES + (i & 1) * TILE_BYTES, F.coeff_map, st.tx0 + F.pad,
+                                       st.ty0 + F.pad, bar);
+                }
+                if (lane < 4) {
+                    const FInfo fi = cached ? s_fi[m.s] : frame_info(C.fs + m.f);
+                    cr.u = __ldcg(nbuf(F, fi.iu) + m.nd);
+                    cr.g = fi.mode != 0 ? __ldcg(nbuf(F, 2 + fi.igc) + m.nd) : make_float2(0.f, 0.f);
+                    cr.d = fi.mode == 1 ? __ldcg(nbuf(F, 5 + fi.idp) + m.nd) : make_float2(0.f, 0.f);
+                }
+                return st;
+            };
+            ChunkMeta m0{}, m1{}, m2{};
+            CandRaw r0{}, r1{};
+            Stage st0{}, st1{};
+            int *sig = nullptr;   // deferred group count of the warp's previous chunk (lanes 0..3)
+            if (gw < total) {
+                m0 = fetch_meta(gw);
+                st0 = issue(m0, pipe_i, r0);
+                if (gw + nw < total) m1 = fetch_meta(gw + nw);
             }
+            for (int g = gw; g < total; g += nw) {
+                const bool has1 = g + nw < total;
+                if (g + 2 * nw < total) m2 = fetch_meta(g + 2 * nw);
+                if (has1) st1 = issue(m1, pipe_i + 1, r1);
+                const bool got = mbar_wait(&s_bar[wid][pipe_i & 1], (pipe_i >> 1) & 1u);
+                if (!__all_sync(0xffffffffu, got)) {
+                    if (lane == 0) {
+                        C.h->err = D2IC_WAIT_TIMEOUT;
+                        atomicExch(&C.h->abort, 1);
+                    }
+                    if (has1) mbar_wait(&s_bar[wid][(pipe_i + 1) & 1], ((pipe_i + 1) >> 1) & 1u);   // bounded
+                    break;
+                }
+                float2 uc = make_float2(0.f, 0.f);
+                if (lane < 4) {
+                    const FInfo fi = cached ? s_fi[m0.s] : frame_info(C.fs + m0.f);
+                    float2 dir;
+                    uc = cand_value(r0.u, r0.g, r0.d, fi.alpha, fi.beta, fi.mode, dir);
+                }
+                chunk_compute<KIND>(frames[m0.f], m0, uc, st0,
+                                    reinterpret_cast<const uint4 *>(wbuf + (pipe_i & 1) * CHUNK_BYTES),
+                                    reinterpret_cast<const float *>(wbuf + 2 * CHUNK_BYTES + (pipe_i & 1) * TILE_BYTES),
+                                    lane, sig);
+                ++pipe_i;
+                m0 = m1;
+                r0 = r1;
+                st0 = st1;
+                m1 = m2;
+            }
+            if (sig) red_release_add(sig, 1);          // the last chunk's counts
+            if (trr) trace[7 * round + 1] = gtimer();
+            // ---- N work: group gi of the active list goes to global warp gi mod (warps in grid); the
+            // warp waits until every chunk with a node in the group has written its slots ----
+            const int tg = ld_vol(&C.h->total_groups);
+            int gcur = 0;
+            for (int gi = gw; gi < tg; gi += nw) {
+                int s, f, base;
+                if (cached) {
+                    while (gcur + 1 < na && s_gpre[gcur + 1] <= gi) ++gcur;
+                    s = gcur;
+                    f = s_act[s];
+                    base = s_gpre[s];
+                } else {
+                    s = find_slot(C.gpre, na, gi);
+                    f = __ldcg(C.active + s);
+                    base = __ldcg(C.gpre + s);
+                }
+                const d2ic_frame_t &F = frames[f];
+                const int g = gi - base;
+                int ok = 1;
+                if (lane == 0) {
+                    const int need = __ldg(F.group_need + g);
+                    const unsigned *cnt = reinterpret_cast<const unsigned *>(F.group_cnt + g);
+                    if ((int)ld_acquire_u32(cnt) < need) {
+                        const unsigned long long t0 = gtimer();
+                        while ((int)ld_acquire_u32(cnt) < need) {
+                            if (ld_vol(&C.h->abort)) {
+                                ok = 0;
+                                break;
+                            }
+                            if (gtimer() - t0 > WAIT_NS) {
+                                C.h->err = D2IC_WAIT_TIMEOUT;
+                                atomicExch(&C.h->abort, 1);
+                                ok = 0;
+                                break;
+                            }
+                            __nanosleep(32);
+                        }
+                    }
+                }
+                __syncwarp();                          // the slots seen by lane 0 are seen by the warp
+                if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+                const FInfo fi = cached ? s_fi[s] : frame_info(C.fs + f);
+                DF q[5];
+                node_work(F, fi, g, lane, q);
+#pragma unroll
+                for (int i = 0; i < 5; ++i) q[i] = df_warp_sum(q[i]);
+                // group -> supergroup (32 groups) -> frame: the warp that completes a level reduces it
+                const int ngr = F.n_groups, nsg = (ngr + GN - 1) / GN, sg = g / GN;
+                float2 *gp = reinterpret_cast<float2 *>(F.group_part);
+                int last = 0;
+                if (lane == 0) {
+#pragma unroll
+                    for (int i = 0; i < 5; ++i) gp[(size_t)g * D2IC_NPART + i] = make_float2(q[i].hi, q[i].lo);
+                    F.group_cnt[g] = 0;                // every chunk of this round has counted
+                    const int members = min(GN, ngr - sg * GN);
+                    last = atom_acq_rel_add(F.group_cnt + ngr + sg, 1) == members - 1;
+                    if (last) F.group_cnt[ngr + sg] = 0;
+                }
+                __syncwarp();
+                if (__shfl_sync(0xffffffffu, last, 0)) {
+                    DF v[5];
+                    const int gg = sg * GN + lane;
+#pragma unroll
+                    for (int i = 0; i < 5; ++i) {
+                        const float2 t = gg < ngr ? __ldcg(gp + (size_t)gg * D2IC_NPART + i) : make_float2(0.f, 0.f);
+                        v[i] = df_warp_sum(DF{t.x, t.y});
+                    }
+                    int lastf = 0;
+                    if (lane == 0) {
+                        float2 *sp = gp + (size_t)(ngr + sg) * D2IC_NPART;
+#pragma unroll
+                        for (int i = 0; i < 5; ++i) sp[i] = make_float2(v[i].hi, v[i].lo);
+                        lastf = atom_acq_rel_add(F.group_cnt + ngr + nsg, 1) == nsg - 1;
+                        if (lastf) F.group_cnt[ngr + nsg] = 0;
+                    }
+                    __syncwarp();
+                    if (__shfl_sync(0xffffffffu, lastf, 0)) {   // the frame's last supergroup
+                        const bool rt = trace != nullptr && lane == 0 && round < trace_rounds;
+                        if (rt) trace[7 * round + 3] = gtimer();
+                        frame_r(F, f, C, eval_only, lane);
+                        if (rt) trace[7 * round + 4] = gtimer();
+                    }
+                }
+            }
+            if (trr) trace[7 * round + 2] = gtimer();
         }
-        if (trr) trace[7 * round + 2] = gtimer();
+        // ---- end of round: the last block to arrive rebuilds the active list if a frame finished ----
         if (!grid_barrier(C.h, [&] {
-                const bool rt = trace != nullptr && threadIdx.x == 0 && round < trace_rounds;
-                if (rt) trace[7 * round + 3] = gtimer();
-                r_step(frames, n_frames, C, eval_only);
-                if (rt) trace[7 * round + 4] = gtimer();
+                if (ld_vol(&C.h->finished)) {
+                    rebuild_active(frames, n_frames, C);
+                    if (threadIdx.x == 0) C.h->finished = 0;
+                }
             }))
             break;
         if (trr) trace[7 * round + 5] = gtimer();
@@ -782,7 +1076,7 @@ finish:
         const int iu = ld_vol(&S->iu), igc = ld_vol(&S->igc);
         const int nn = F.n_nodes;
         float2 *uo = reinterpret_cast<float2 *>(F.u_out);
-        for (int i = blockIdx.x * NG + threadIdx.x; i < nn; i += gridDim.x * NG) {
+        for (int i = blockIdx.x * NT + threadIdx.x; i < nn; i += gridDim.x * NT) {
             if (uo) uo[i] = __ldcg(nbuf(F, iu) + i);
             if (eval_only && grad_out && f == 0) reinterpret_cast<float2 *>(grad_out)[i] = __ldcg(nbuf(F, 2 + igc) + i);
         }
@@ -802,13 +1096,13 @@ finish:
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-constexpr size_t ENGINE_SMEM = sizeof(float) * NWARP * TILE_CAP;   // per-warp coefficient tiles
+constexpr size_t ENGINE_SMEM = (size_t)NWARP * WARP_SMEM;   // per warp: 2 record + 2 tile buffers
 
 template <int KIND>
 static cudaError_t occupancy(int *blocks_per_sm) {
     cudaError_t e = cudaFuncSetAttribute(cg_engine<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ENGINE_SMEM);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cg_engine<KIND>, NG, ENGINE_SMEM);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cg_engine<KIND>, NT, ENGINE_SMEM);
 }
 
 struct DevInfo {
@@ -862,7 +1156,7 @@ static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control
     // cooperative launch through cudaLaunchKernelEx (co-residency checked by the driver; capturable)
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(blocks);
-    cfg.blockDim = dim3(NG);
+    cfg.blockDim = dim3(NT);
     cfg.dynamicSmemBytes = ENGINE_SMEM;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -890,14 +1184,33 @@ extern "C" size_t d2ic_cg_control_bytes(int n_frames) {
     return ctl_layout(n_frames, &a, &b, &c, &d);
 }
 
+// Workspace of one frame: 7 node buffers (u x2, g x3, dir x2), the K gradient
+// slots per node (16 bytes: gx, gy and the chunk's r^2 sum as a double-float),
+// the partials (D2IC_NPART double-float pairs) of every group and then of every
+// supergroup of 32 groups, the completion counters (groups, supergroups, the
+// frame's count of supergroups), and the tile origins.
+static size_t ws_layout(int n_nodes, int n_chunks, int node_chunk_k, size_t off[5]) {
+    const size_t ng = (size_t)(n_nodes + GN - 1) / GN;
+    size_t o = 0;
+    off[0] = o;                                               // node_ws
+    o += align256(sizeof(float) * 14 * (size_t)n_nodes);
+    off[1] = o;                                               // node_grad
+    o += align256(sizeof(float) * 4 * (size_t)node_chunk_k * n_nodes);
+    off[2] = o;                                               // group_part
+    const size_t ns = (ng + GN - 1) / GN;                     // supergroups of GN groups
+    o += align256(sizeof(float) * 2 * D2IC_NPART * (ng + ns));
+    off[3] = o;                                               // group_cnt
+    o += align256(sizeof(int) * (ng + ns + 1));
+    off[4] = o;                                               // chunk_tile
+    o += align256(sizeof(int) * (size_t)(n_chunks > 0 ? n_chunks : 1));
+    return o;
+}
+
 extern "C" size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks, int node_chunk_k) {
-    const int ng = (n_nodes + NG - 1) / NG;
+    size_t off[5];
     if (node_chunk_k < 1) node_chunk_k = 1;
-    size_t off = align256(sizeof(float) * 14 * (size_t)n_nodes);
-    off += align256(sizeof(double) * (size_t)n_chunks);
-    off += align256(sizeof(float) * 2 * (size_t)node_chunk_k * n_nodes);
-    off += align256(sizeof(double) * D2IC_NPART * (size_t)(ng > 0 ? ng : 1));
-    return off;
+    if (n_nodes < 1) n_nodes = 1;
+    return ws_layout(n_nodes, n_chunks, node_chunk_k, off);
 }
 
 extern "C" int d2ic_frame_bind_workspace(d2ic_frame_t *f, void *ws) {
@@ -905,16 +1218,78 @@ extern "C" int d2ic_frame_bind_workspace(d2ic_frame_t *f, void *ws) {
     D2IC_REQUIRE(((uintptr_t)ws & 255) == 0, "d2ic_frame_bind_workspace: workspace must be 256-byte aligned");
     D2IC_REQUIRE(f->n_nodes >= 1 && f->n_chunks >= 0 && f->node_chunk_k >= 1 && f->node_chunk_k <= 255,
                  "d2ic_frame_bind_workspace: bad sizes");
+    size_t off[5];
+    ws_layout(f->n_nodes, f->n_chunks, f->node_chunk_k, off);
     char *p = (char *)ws;
-    f->node_ws = (float *)p;
-    p += align256(sizeof(float) * 14 * (size_t)f->n_nodes);
-    f->chunk_J = (double *)p;
-    p += align256(sizeof(double) * (size_t)f->n_chunks);
-    f->node_grad = (float *)p;
-    p += align256(sizeof(float) * 2 * (size_t)f->node_chunk_k * f->n_nodes);
-    f->group_part = (double *)p;
-    f->n_groups = (f->n_nodes + NG - 1) / NG;
-    f->chunks_per_group = (f->n_chunks + f->n_groups - 1) / f->n_groups;
+    f->node_ws = (float *)(p + off[0]);
+    f->node_grad = (float *)(p + off[1]);
+    f->group_part = (float *)(p + off[2]);
+    f->group_cnt = (int *)(p + off[3]);
+    f->chunk_tile = (int *)(p + off[4]);
+    f->n_groups = (f->n_nodes + GN - 1) / GN;
+    return D2IC_OK;
+}
+
+// Tensor-map encoding comes from the driver through the runtime's entry-point
+// query, so the library does not link libcuda directly.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+extern "C" int d2ic_frame_encode_tiles(d2ic_frame_t *f, int tile_w, int tile_h) {
+    static_assert(sizeof(d2ic_frame_t) % 64 == 0, "descriptor arrays keep every tensor map 64-byte aligned");
+    static_assert(offsetof(d2ic_frame_t, coeff_map) == 0 && sizeof(f->coeff_map) == sizeof(CUtensorMap),
+                  "tensor map first in the descriptor");
+    D2IC_REQUIRE(f, "d2ic_frame_encode_tiles: null frame");
+    memset(f->coeff_map, 0, sizeof(f->coeff_map));
+    f->tile_w = 0;
+    f->tile_h = 0;
+    if (tile_w == 0) return D2IC_OK;
+    D2IC_REQUIRE(tile_w >= 4 && tile_w % 4 == 0 && tile_h >= 4 && tile_w <= 256 && tile_h <= 256 &&
+                     tile_w * tile_h <= D2IC_TILE_MAX_FLOATS,
+                 "d2ic_frame_encode_tiles: tile %d x %d (width a multiple of 4, at most %d floats)", tile_w, tile_h,
+                 D2IC_TILE_MAX_FLOATS);
+    D2IC_REQUIRE(f->coeff && ((uintptr_t)f->coeff & 15) == 0, "d2ic_frame_encode_tiles: coeff must be 16-byte aligned");
+    D2IC_REQUIRE(f->pad % 4 == 0 && f->cpitch % 4 == 0 && f->W >= 1 && f->H >= 1 && f->cpitch >= f->W + 2 * f->pad,
+                 "d2ic_frame_encode_tiles: pad and cpitch must be multiples of 4 (pad %d, cpitch %d)", f->pad,
+                 f->cpitch);
+    D2IC_REQUIRE(f->W + 2 * f->pad < 32768 && f->H + 2 * f->pad < 32768,
+                 "d2ic_frame_encode_tiles: image %d x %d too large for tile origins", f->W, f->H);
+    EncodeTiledFn fn = encode_tiled_fn();
+    if (!fn) {
+        set_error("d2ic_frame_encode_tiles: the driver provides no cuTensorMapEncodeTiled");
+        return D2IC_UNSUPPORTED;
+    }
+    alignas(64) CUtensorMap map;
+    const cuuint64_t dims[2] = {(cuuint64_t)(f->W + 2 * f->pad), (cuuint64_t)(f->H + 2 * f->pad)};
+    const cuuint64_t strides[1] = {(cuuint64_t)f->cpitch * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)tile_w, (cuuint32_t)tile_h};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)f->coeff, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("d2ic_frame_encode_tiles: cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return D2IC_CUDA_ERROR;
+    }
+    memcpy(f->coeff_map, &map, sizeof(map));
+    f->tile_w = tile_w;
+    f->tile_h = tile_h;
     return D2IC_OK;
 }
 

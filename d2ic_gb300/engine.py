@@ -172,6 +172,13 @@ class FrameLayout:
         r4 = rank.reshape(-1, 4)
         chunk_slot = (r4[:, 0] | (r4[:, 1] << 8) | (r4[:, 2] << 16) | (r4[:, 3] << 24)).astype(np.uint32).view(np.int32)
         self.node_chunk_k = K
+        # chunks with a node in each group of NODE_GROUP consecutive nodes (the group's reducer
+        # waits for that many completion counts per pass)
+        ng = (self.n_nodes + _lib.NODE_GROUP - 1) // _lib.NODE_GROUP
+        cg = np.sort(chunk_nodes.astype(np.int64).reshape(-1, 4) // _lib.NODE_GROUP, axis=1)
+        first = np.ones(cg.shape, dtype=bool)
+        first[:, 1:] = cg[:, 1:] != cg[:, :-1]
+        group_need = np.bincount(cg[first], minlength=ng).astype(np.int32)
         # spring table: entries beyond the degree are padding; column-major for coalesced node-pass loads
         nbi = np.asarray(pix.node_neighbor_index, dtype=np.int64).reshape(self.n_nodes, -1)
         md = nbi.shape[1]
@@ -193,6 +200,7 @@ class FrameLayout:
         self.chunk_nodes = T(chunk_nodes)
         self.chunk_box = T(chunk_box) if self.n_chunks else torch.zeros((1, 2), dtype=torch.int32, device=dev)
         self.chunk_slot = T(chunk_slot) if self.n_chunks else torch.zeros((1,), dtype=torch.int32, device=dev)
+        self.group_need = T(group_need)
         self.nbr_index = T(nbr_index) if md else torch.full((1,), -1, dtype=torch.int32, device=dev)
         self.nbr_weight = T(nbr_weight) if md else torch.zeros((1,), dtype=torch.float32, device=dev)
         self.pixel_order = order
@@ -205,6 +213,19 @@ class FrameLayout:
                       self.kind, ptr(self.pix), _lib.stream_handle())
         self.ref_image = ref
         del ref_coeff
+        # shared-memory coefficient tile per chunk (cubic): the chunk's largest pixel box plus the
+        # 4x4 stencil (3), a 2-pixel margin each side (4), one pixel of spread between the
+        # element's nodes (1) and, in x, up to 3 columns lost to the 16-byte TMA alignment
+        self.tile_w = self.tile_h = 0
+        if self.kind == _lib.INTERP_CUBIC and self.n_chunks and self.W + 2 * PAD < 32768 and self.H + 2 * PAD < 32768:
+            b0 = chunk_box[:, 0].astype(np.int64) & 0xFFFFFFFF
+            b1 = chunk_box[:, 1].astype(np.int64) & 0xFFFFFFFF
+            cw = int(((b1 & 0xFFFF) - (b0 & 0xFFFF)).max()) + 1
+            ch = int(((b1 >> 16) - (b0 >> 16)).max()) + 1
+            tw = (cw + 11 + 3) // 4 * 4
+            th = ch + 8
+            if tw * th <= _lib.TILE_MAX_FLOATS:
+                self.tile_w, self.tile_h = tw, th
 
     # bytes read per pixel per objective evaluation by the P phase (pixel record + ~1 coefficient)
     PIX_BYTES = 16 + 4
@@ -237,6 +258,7 @@ class FrameSlot:
         f.chunk_nodes = ptr(L.chunk_nodes)
         f.chunk_box = ptr(L.chunk_box)
         f.chunk_slot = ptr(L.chunk_slot)
+        f.group_need = ptr(L.group_need)
         f.node_chunk_k = L.node_chunk_k
         f.nbr_index = ptr(L.nbr_index)
         f.nbr_weight = ptr(L.nbr_weight)
@@ -252,6 +274,9 @@ class FrameSlot:
         f.W, f.H, f.cpitch, f.pad = L.W, L.H, L.cpitch, PAD
         f.n_pix, f.n_chunks, f.n_nodes, f.max_deg = L.n_pix, L.n_chunks, L.n_nodes, L.max_deg
         _lib.call("d2ic_frame_bind_workspace", ctypes.byref(f), ptr(self.ws))
+        rc = _lib.load().d2ic_frame_encode_tiles(ctypes.byref(f), L.tile_w, L.tile_h)
+        if rc not in (_lib.OK, _lib.UNSUPPORTED):      # unsupported: taps through L1, same results
+            _lib.check(rc)
         return f
 
     def set_params(self, tol: float, alpha_reg: float):
@@ -308,15 +333,16 @@ class Engine:
                   grid_blocks, int(max_rounds), _lib.stream_handle(stream))
 
     def solve_traced(self, desc_dev: torch.Tensor, n_frames: int, kind: int, rounds: int = 4096, grid_blocks: int = 0):
-        """Solve; per-round durations in microseconds: block 0's own pixel work, its wait at the
-        pixel-pass barrier, its node pass, wait until the control step starts, control step, release."""
+        """Solve; per-round durations in microseconds, columns: warp 0 of block 0's pixel work, its
+        node-group work, from there to the end of the round, the (last) frame control step, from
+        that step to the end of the round, and the whole round."""
         tr = torch.zeros(7 * rounds, dtype=torch.int64, device=self.device)
         _lib.call("d2ic_cg_solve_traced", ptr(desc_dev), n_frames, ptr(self.control), self.control.numel(), kind,
                   grid_blocks, ptr(tr), rounds, _lib.stream_handle())
         t = tr.cpu().numpy().reshape(-1, 7).astype(np.float64)
         t = t[t[:, 5] > 0]
-        return np.stack([t[:, 6] - t[:, 0], t[:, 1] - t[:, 6], t[:, 2] - t[:, 1], t[:, 3] - t[:, 2],
-                         t[:, 4] - t[:, 3], t[:, 5] - t[:, 4]], axis=1) / 1e3
+        return np.stack([t[:, 1] - t[:, 0], t[:, 2] - t[:, 1], t[:, 5] - t[:, 2], t[:, 4] - t[:, 3],
+                         t[:, 5] - t[:, 4], t[:, 5] - t[:, 0]], axis=1) / 1e3
 
     def eval_objective(self, desc_dev: torch.Tensor, u: torch.Tensor, kind: int, stream=None):
         J = torch.zeros(1, dtype=torch.float64, device=self.device)

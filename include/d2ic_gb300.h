@@ -44,10 +44,11 @@ extern "C" {
 #define D2IC_INTERP_LINEAR  1   /* bilinear, edge clamped                     */
 
 /* sizes of the engine's fixed-shape pieces */
-#define D2IC_NODE_GROUP   512   /* nodes per reduction group (= block size)   */
-#define D2IC_NPART          6   /* doubles per group partial                  */
+#define D2IC_NODE_GROUP    32   /* nodes per reduction group (one warp)       */
+#define D2IC_NPART          5   /* double-float pairs per group partial       */
 #define D2IC_MAX_FRAMES  4096   /* frames per batched launch                  */
 #define D2IC_CHUNK_MAX    256   /* pixels per chunk (one element per chunk)   */
+#define D2IC_TILE_MAX_FLOATS 736 /* largest staged coefficient tile (w x h)  */
 
 /* One pixel of the element-major pixel list: 16 bytes, read with one 128-bit load. */
 typedef struct d2ic_pixrec {
@@ -62,6 +63,11 @@ typedef struct d2ic_pixrec {
  * pointers.  The workspace fields are set by d2ic_frame_bind_workspace().
  */
 typedef struct d2ic_frame {
+    /* TMA tensor map (a CUtensorMap, 128 bytes) of `coeff`, written by
+     * d2ic_frame_encode_tiles(); it is read by the kernels from the device copy
+     * of the descriptor, which must therefore be 64-byte aligned (sizeof is a
+     * multiple of 64, so every element of a 64-byte aligned array is) */
+    uint64_t     coeff_map[16];
     /* deformed image: B-spline coefficients (cubic) or the image itself (linear),
      * with a `pad`-wide halo; pixel (i,j) lives at coeff[(i+pad)*cpitch + j+pad] */
     const float *coeff;
@@ -74,6 +80,8 @@ typedef struct d2ic_frame {
     const int   *chunk_slot;       /* n_chunks: byte a = rank of the chunk among the chunks
                                       of its local node a (ascending chunk order), i.e.
                                       the node_grad slot the chunk's partial goes to     */
+    const int   *group_need;       /* n_groups: chunks with a node in group g (nodes
+                                      D2IC_NODE_GROUP*g ... +D2IC_NODE_GROUP-1)          */
     const int   *nbr_index;        /* max_deg * n_nodes spring neighbours, column-major,
                                       -1 padded after the last neighbour                */
     const float *nbr_weight;       /* same layout: w_ij * (rho_i + rho_j) / 2           */
@@ -85,24 +93,34 @@ typedef struct d2ic_frame {
     int         *n_evals;          /* 1: objective evaluations (pixel passes) performed */
     /* workspace */
     float       *node_ws;          /* 14 * n_nodes floats                               */
-    double      *chunk_J;          /* n_chunks x 8 bytes: each chunk's sum of r^2 as a
-                                      double-float (hi, lo) pair                         */
-    float       *node_grad;        /* 2 * node_chunk_k * n_nodes: per-node slots of the
-                                      chunks' gradient partials, column-major (slot k of
-                                      node n at k * n_nodes + n), unused slots stay 0    */
-    double      *group_part;       /* D2IC_NPART * n_groups                             */
+    float       *node_grad;        /* 4 * node_chunk_k * n_nodes: per-node slots of the
+                                      chunks' partials (gx, gy, and for the chunk's node 0
+                                      its sum of r^2 as a double-float hi, lo), column-major
+                                      (slot k of node n at k * n_nodes + n), unused slots 0 */
+    float       *group_part;       /* 2 * D2IC_NPART * (n_groups + n_super) double-float
+                                      partials of the groups, then of the supergroups of
+                                      32 groups (n_super = ceil(n_groups / 32))          */
+    int         *group_cnt;        /* n_groups + n_super + 1 completion counters (all 0
+                                      between rounds)                                   */
+    int         *chunk_tile;       /* n_chunks: origin (col | row << 16, int16 each) of the
+                                      chunk's coefficient tile for the next pass        */
     double       tol;
     float        alpha_reg;
     int          max_iter;
     int          W, H, cpitch, pad;
     int          n_pix, n_chunks, n_nodes, max_deg;
-    int          n_groups, chunks_per_group;
-    int          node_chunk_k, reserved_;
+    int          n_groups;         /* set by d2ic_frame_bind_workspace                  */
+    int          node_chunk_k;
+    int          tile_w, tile_h;   /* staged coefficient tile (0 = taps read from global
+                                      memory); set by d2ic_frame_encode_tiles()         */
+    int          reserved_[8];
 } d2ic_frame_t;
 
 /* ---- library ------------------------------------------------------------- */
 D2IC_API const char *d2ic_last_error_string(void);
 D2IC_API int d2ic_version(void);
+/* sizeof(d2ic_frame_t), for bindings that mirror the descriptor to check their layout. */
+D2IC_API size_t d2ic_frame_descriptor_bytes(void);
 /* SM count and the persistent engine's resident blocks per SM on `device`. */
 D2IC_API int d2ic_device_info(int device, int *num_sms, int *engine_blocks_per_sm);
 
@@ -137,6 +155,16 @@ D2IC_API int d2ic_pack_pixels(const int *colrow, const float *xieta, int n,
  * descriptor (host-side; `ws` is a device pointer aligned to 256 bytes). */
 D2IC_API size_t d2ic_frame_workspace_bytes(int n_nodes, int n_chunks, int node_chunk_k);
 D2IC_API int d2ic_frame_bind_workspace(d2ic_frame_t *frame, void *ws);
+
+/* Stage each chunk's window of the coefficient image in shared memory with a
+ * 2-D TMA copy of tile_w x tile_h floats (tile_w a multiple of 4,
+ * tile_w * tile_h <= D2IC_TILE_MAX_FLOATS, cubic frames only): encodes
+ * frame->coeff_map for frame->coeff, W, H, cpitch and pad, which must be set.
+ * tile_w = 0 turns staging off (taps read through L1).  Host-side.  Pixels
+ * that fall outside their chunk's tile read global memory, with the same
+ * arithmetic, so results do not depend on the tile shape.  Returns
+ * D2IC_UNSUPPORTED (staging off) when the driver lacks tensor-map encoding. */
+D2IC_API int d2ic_frame_encode_tiles(d2ic_frame_t *frame, int tile_w, int tile_h);
 
 /* Bytes of launch-wide control scratch for a batched launch of n_frames. */
 D2IC_API size_t d2ic_cg_control_bytes(int n_frames);
