@@ -60,6 +60,13 @@ def parse():
     p.add_argument("--serve-frames", type=int, default=4)
     p.add_argument("--serve-slots", type=int, default=32)
     p.add_argument("--serve-slice", type=int, default=16)
+    p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--batch-frames", type=int, default=64)
+    p.add_argument("--batch-sides", default="512,1024,2048",
+                   help="image sides drawn for the uneven batch (the full set adds 3072,4096)")
+    p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--adjoint-realisations", type=int, default=256)
+    p.add_argument("--adjoint-fd-dirs", type=int, default=32)
     return p.parse_args()
 
 
@@ -225,7 +232,7 @@ def run_reference(args, ws, rank):
 # served vs plain on a mixed stream
 # ---------------------------------------------------------------------------
 
-def run_serving(args, dev):
+def run_serving(args, dev, sides=(512, 1024, 2048), n_seq=None, label="mixed_stream"):
     """Plain single-frame drop-in vs the continuous-batching server on the same requests."""
     import torch
 
@@ -233,7 +240,8 @@ def run_serving(args, dev):
     from d2ic_gb300 import workloads
     from d2ic_gb300.serving import DICServer, Request, ServeConfig
 
-    seqs = workloads.mixed_stream(n_seq=args.serve_seqs, frames_per_seq=args.serve_frames, device=dev)
+    seqs = workloads.mixed_stream(n_seq=n_seq or args.serve_seqs, frames_per_seq=args.serve_frames, device=dev,
+                                  sides=tuple(sides))
     F = args.serve_frames
     order = [(s, k) for k in range(F) for s in range(len(seqs))]
     pinned = [[torch.from_numpy(f).pin_memory() for f in wl.frames] for wl in seqs]
@@ -270,7 +278,7 @@ def run_serving(args, dev):
     plain_u, plain_lat = plain_pass()
     t_plain = time.perf_counter() - t0
 
-    srv = DICServer(dev, ServeConfig(max_slots=args.serve_slots, slice_rounds=args.serve_slice))
+    srv = DICServer(dev, ServeConfig(max_slots=args.serve_slots, slice_rounds=args.serve_slice, autotune=True))
     for s, wl in enumerate(seqs):
         srv.add_sequence(s, wl.ref, wl.mesh, wl.assets, wl.config, init=wl.init)
 
@@ -300,7 +308,7 @@ def run_serving(args, dev):
     offsets = np.cumsum(rng.exponential(1.0 / rate, len(order)))
     reqs_on = served_pass(offsets)
     lat = np.array([r.latency for r in reqs_on])
-    return {"workload": "mixed_stream", "sequences": len(seqs), "frames": len(order),
+    return {"workload": label, "sequences": len(seqs), "frames": len(order),
             "image_sides": sorted({int(wl.ref.shape[0]) for wl in seqs}), "roi_pixels_per_pass": int(n_pix),
             "plain_frames_per_s": len(order) / t_plain, "served_frames_per_s": served_fps,
             "speedup": served_fps / (len(order) / t_plain), "max_abs_diff_vs_plain_px": diff,
@@ -309,6 +317,158 @@ def run_serving(args, dev):
             "online_rate_frames_per_s": rate, "latency_ms_p50": 1000 * float(np.percentile(lat, 50)),
             "latency_ms_p99": 1000 * float(np.percentile(lat, 99)), "slots": args.serve_slots,
             "slice_rounds": args.serve_slice, "graphs": srv.graph is not None}
+
+
+# ---------------------------------------------------------------------------
+# uneven frames in one persistent launch
+# ---------------------------------------------------------------------------
+
+def run_batched(args, dev):
+    """64 independent frames of uneven size: one batched launch vs one launch per frame."""
+    import torch
+
+    from d2ic_gb300 import workloads
+    from d2ic_gb300.autotune import default_tuner
+    from d2ic_gb300.engine import Engine, FrameLayout, FrameSlot, as_device_image, descriptors_to_device
+
+    sides = tuple(int(x) for x in args.batch_sides.split(","))
+    t0 = time.perf_counter()
+    wls = workloads.uneven_batch(args.batch_frames, device=dev, sides=sides)
+    t_assets = time.perf_counter() - t0
+    tuner = default_tuner(dev)
+    slots, shapes = [], []
+    t0 = time.perf_counter()
+    for wl in wls:
+        ref = as_device_image(wl.ref, dev)
+        shape = tuner.tune(wl.assets.pixel_data, wl.n_nodes, ref, torch.roll(ref, 1, dims=1), "cubic")
+        shapes.append(shape.chunk_pixels)
+        lay = FrameLayout(wl.assets.pixel_data, wl.n_nodes, wl.ref, "cubic", dev, chunk_max=shape.chunk_pixels)
+        sl = FrameSlot(lay, wl.config.max_iters)
+        sl.set_params(wl.config.tol, wl.config.reg_strength)
+        sl.load_image(wl.frames[0])
+        sl.set_u0(None)
+        slots.append(sl)
+    t_tune = time.perf_counter() - t0
+    n = len(slots)
+    desc_all = descriptors_to_device([s.desc for s in slots], dev)
+    desc_one = [descriptors_to_device([s.desc], dev) for s in slots]
+    eng = Engine(dev, n)
+    eng1 = Engine(dev, 1)
+
+    def batched():
+        eng.solve(desc_all, n, slots[0].layout.kind)
+
+    def one_by_one():
+        for d in desc_one:
+            eng1.solve(d, 1, slots[0].layout.kind)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1000.0)
+        return statistics.median(ts)
+
+    t_one = timed(one_by_one, max(1, args.steps))
+    u_one = [s.u_out.clone() for s in slots]
+    it_one = [int(s.info[0]) for s in slots]
+    t_b = timed(batched, max(1, args.steps))
+    diff = max(float((s.u_out - u).abs().max()) for s, u in zip(slots, u_one))
+    same_iters = all(int(s.info[0]) == k for s, k in zip(slots, it_one))
+    n_pix = sum(wl.n_pix for wl in wls)
+    evals = sum(int(s.info[2]) for s in slots)
+    bytes_eval = sum(int(s.info[2]) * (B_PIX * wl.n_pix + B_NODE * wl.n_nodes) for s, wl in zip(slots, wls))
+    peak, _ = peaks()
+    return {"workload": "uneven_batch", "frames": n, "image_sides": sorted(set(int(w.ref.shape[0]) for w in wls)),
+            "elements_px": sorted(set(int(w.name.split("_e")[1]) for w in wls)), "roi_pixels": n_pix,
+            "batched_frames_per_s": n / t_b, "one_launch_per_frame_frames_per_s": n / t_one,
+            "speedup": t_one / t_b, "batched_ms": 1000 * t_b, "one_by_one_ms": 1000 * t_one,
+            "max_abs_diff_batched_vs_alone_px": diff, "same_iterations": same_iters,
+            "objective_evaluations": evals,
+            "roofline_frac_batched": (bytes_eval / 1e9 / t_b) / peak,
+            "chunk_pixels_chosen": {str(c): shapes.count(c) for c in sorted(set(shapes))},
+            "setup_s": {"assets": round(t_assets, 2), "autotune_and_layouts": round(t_tune, 2)}}
+
+
+# ---------------------------------------------------------------------------
+# implicit adjoint: noise propagation and finite differences
+# ---------------------------------------------------------------------------
+
+def run_adjoint(args, dev):
+    """du*/dI2 for image-noise realisations (sigma 2) and its strain sensitivity, checked by FD."""
+    import torch
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300 import workloads
+    from d2ic_gb300.adjoint import ImplicitAdjoint, newton_polish, strain_jvp
+    from d2ic_gb300.mesh_assets import build_node_neighbor_tables
+
+    wl = workloads.uniaxial_1024(device=dev)
+    H, W = wl.ref.shape
+    solver = d2.GlobalCGSolver(device=dev)
+    dic = d2.DICMeshBased(wl.mesh, solver, wl.config)
+    dic.prepare(wl.ref, wl.assets)
+    img = torch.as_tensor(wl.frames[0], device=dev)
+    res = dic.run(wl.frames[0])
+    alpha = wl.config.reg_strength
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u = newton_polish(solver, dic.state, img, res.u_nodal, alpha, steps=2)
+    slot = solver._ensure(dic.state)
+    slot.load_image(img)
+    adj = ImplicitAdjoint(slot, u, alpha)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    R = args.adjoint_realisations
+    g = torch.Generator(device=dev).manual_seed(3000)
+    noise = 2.0 * torch.randn((R, H, W), generator=g, device=dev, dtype=torch.float32)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    du = adj.jvp(noise, rtol=1e-6)
+    torch.cuda.synchronize()
+    t_jvp = time.perf_counter() - t0
+    jvp_iters = adj.last_iters
+    idx, deg = build_node_neighbor_tables(wl.mesh)
+    dE = strain_jvp(u, du, np.asarray(wl.mesh.nodes_xy), idx, deg)
+    used = torch.as_tensor(np.unique(np.asarray(wl.mesh.elements)), device=dev)
+    u_std = du[:, used].std(dim=0)
+    e_std = dE[:, used].std(dim=0)
+    # VJP timing (one cotangent)
+    gu = torch.zeros((1,) + tuple(u.shape), dtype=torch.float64, device=dev)
+    gu[0, used, 0] = 1.0 / used.numel()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    adj.vjp(gu, rtol=1e-6)
+    torch.cuda.synchronize()
+    t_vjp = time.perf_counter() - t0
+    # central finite differences of the exactly converged solution (Newton from u*)
+    h = 1e-2
+    D = args.adjoint_fd_dirs
+    gd = torch.Generator(device=dev).manual_seed(3100)
+    rels = []
+    t0 = time.perf_counter()
+    for k in range(D):
+        d = torch.randn((1, H, W), generator=gd, device=dev, dtype=torch.float32)
+        j = adj.jvp(d, rtol=1e-9)[0].to(torch.float64)
+        up = newton_polish(solver, dic.state, img + h * d[0], u, alpha, steps=2).to(torch.float64)
+        um = newton_polish(solver, dic.state, img - h * d[0], u, alpha, steps=2).to(torch.float64)
+        fd = (up - um) / (2 * h)
+        rels.append(float(torch.linalg.norm((fd - j)[used]) / torch.linalg.norm(j[used])))
+    t_fd = time.perf_counter() - t0
+    slot.load_image(img)
+    return {"workload": "uniaxial_1024", "roi_pixels": wl.n_pix, "nodes": wl.n_nodes, "element_px": 12,
+            "realisations": R, "noise_sigma": 2.0,
+            "jvp_realisations_per_s": R / t_jvp, "jvp_s": t_jvp, "pcg_iterations": jvp_iters,
+            "vjp_s": t_vjp, "setup_s": t_setup,
+            "u_std_px_median": float(u_std.median()), "strain_std_median": [float(v) for v in e_std.median(dim=0).values],
+            "fd_directions": D, "fd_h": h, "fd_rel_err_max": max(rels) if rels else None,
+            "fd_rel_err_median": statistics.median(rels) if rels else None, "fd_s": t_fd}
 
 
 # ---------------------------------------------------------------------------
@@ -424,6 +584,13 @@ def run_ours(args, ws, rank, local):
 
     if not args.no_serve:
         out["serving"] = run_serving(args, dev)
+        # the small-frame regime, where one frame alone cannot fill the GPU
+        out["serving_small_frames"] = run_serving(args, dev, sides=(512,), n_seq=4 * args.serve_seqs,
+                                                  label="small_frame_stream")
+    if not args.no_batch:
+        out["batched"] = run_batched(args, dev)
+    if not args.no_adjoint:
+        out["adjoint"] = run_adjoint(args, dev)
 
     if not args.no_cpu and rank == 0:
         cb = cpu_sequence_sample(wl, args.cpu_sample_frames, u_start=res.u[0].cpu().numpy())

@@ -57,6 +57,7 @@ class ServeConfig:
     slice_rounds: int = 16
     use_graphs: bool = True
     grid_blocks: int = 0
+    autotune: bool = False                   # chunk size per sequence from the launch-shape autotuner
 
 
 @dataclass
@@ -126,13 +127,23 @@ class DICServer:
 
     # -- sequences -----------------------------------------------------------------------------------
     def add_sequence(self, seq_id, ref_image, mesh, assets, config: MeshDICConfig,
-                     init: InitMotionConfig | None = None, chunk_pixels: int = 256):
-        """Make a sequence resident: pixel layout of its reference image and mesh, strain tables."""
+                     init: InitMotionConfig | None = None, chunk_pixels: int | None = None):
+        """Make a sequence resident: pixel layout of its reference image and mesh, strain tables.
+
+        ``chunk_pixels``: pixels per engine chunk; by default the autotuner's choice for the
+        sequence's frame signature when ``ServeConfig.autotune`` is set, else 256."""
         if seq_id in self.seqs:
             raise ValueError(f"sequence {seq_id!r} already registered")
         if assets.pixel_data is None:
             raise ValueError("assets must carry pixel_data (build_pixel_assets)")
         nn = int(np.asarray(mesh.nodes_xy).shape[0])
+        if chunk_pixels is None:
+            chunk_pixels = _lib.CHUNK_MAX
+            if self.cfg.autotune:
+                from .autotune import default_tuner
+                ref = as_device_image(ref_image, self.device)
+                chunk_pixels = default_tuner(self.device).tune(assets.pixel_data, nn, ref, torch.roll(ref, 1, dims=1),
+                                                               self.interpolation).chunk_pixels
         layout = FrameLayout(assets.pixel_data, nn, ref_image, self.interpolation, self.device, chunk_max=chunk_pixels)
         T = lambda a, dt: torch.as_tensor(np.ascontiguousarray(np.asarray(a)), dtype=dt, device=self.device)
         idx, deg = assets.node_neighbor_index, assets.node_neighbor_degree

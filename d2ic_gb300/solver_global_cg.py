@@ -44,7 +44,8 @@ class GlobalCGSolver(SolverBase):
     """Global CG solver for mesh DIC; expects ``MeshAssets.pixel_data``."""
 
     def __init__(self, verbose: bool = False, interpolation: str = "cubic", use_map_coordinates: bool | None = None,
-                 log_cg: bool = False, device=None, grid_blocks: int = 0, chunk_pixels: int = 256) -> None:
+                 log_cg: bool = False, device=None, grid_blocks: int = 0, chunk_pixels: int = 256,
+                 autotune: bool = False) -> None:
         self._compiled = False
         self._verbose = bool(verbose)
         self._log_cg = bool(log_cg)
@@ -57,6 +58,8 @@ class GlobalCGSolver(SolverBase):
         self._device = torch.device(device if device is not None else "cuda")
         self._grid_blocks = int(grid_blocks)
         self._chunk_pixels = int(chunk_pixels)
+        self._autotune = bool(autotune)
+        self.launch_shape = None          # the autotuner's choice, when autotune=True
         self._layout = None
         self._layout_key = None
         self._slot = None
@@ -78,6 +81,15 @@ class GlobalCGSolver(SolverBase):
         key = (id(pix), id(state.ref_image), int(state.config.max_iters))
         if self._layout is None or self._layout_key != key:
             n_nodes = int(np.asarray(assets.mesh.nodes_xy).shape[0])
+            if self._autotune:
+                # probe frame: the reference shifted by one pixel (non-zero residuals, so rounds run)
+                from .autotune import default_tuner
+                from .engine import as_device_image
+                ref = as_device_image(state.ref_image, self._device)
+                shape = default_tuner(self._device).tune(pix, n_nodes, ref, torch.roll(ref, 1, dims=1),
+                                                         self._interpolation)
+                self._chunk_pixels, self._grid_blocks = shape.chunk_pixels, shape.grid_blocks
+                self.launch_shape = shape
             self._layout = FrameLayout(pix, n_nodes, state.ref_image, self._interpolation, self._device,
                                        chunk_max=self._chunk_pixels)
             self._slot = FrameSlot(self._layout, int(state.config.max_iters))

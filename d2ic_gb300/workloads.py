@@ -44,6 +44,22 @@ class Workload:
         return int(np.asarray(self.mesh.nodes_xy).shape[0])
 
 
+def _build_assets(items, elems, workers: int | None = None):
+    """Mesh + pixel assets of (mask, reference image) pairs on host threads (numpy releases the GIL)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    from dataclasses import replace
+
+    def one(arg):
+        (mask, ref), elem = arg
+        mesh, assets = mask_to_mesh_assets(mask, elem)
+        return mesh, replace(assets, pixel_data=build_pixel_assets(mesh, ref, 1.0, assets.roi_mask))
+
+    n = workers or min(16, os.cpu_count() or 1)
+    with ThreadPoolExecutor(max_workers=n) as ex:
+        return list(ex.map(one, zip(items, elems)))
+
+
 def translation_512(seed: int = 0, device="cpu") -> Workload:
     H = W = 512
     warp = Translation(0.35, -0.62)
@@ -70,7 +86,7 @@ def mixed_stream(n_seq: int = 16, frames_per_seq: int = 4, seed: int = 4, device
 
     from .synthetic import Affine, ellipse_mask
     rng = np.random.default_rng(seed)
-    out = []
+    specs = []
     for s in range(n_seq):
         H = int(rng.choice(sides))
         elem = int(rng.choice(elements))
@@ -85,13 +101,12 @@ def mixed_stream(n_seq: int = 16, frames_per_seq: int = 4, seed: int = 4, device
         ref, frames = speckle_sequence(H, H, warps, seed=4000 + s, noise_seeds=[40000 + 100 * s + k for k in
                                                                                  range(frames_per_seq + 1)],
                                        noise_sigma=0.5, device=device)
-        mask = ellipse_mask(H, H, r)
-        mesh, assets = mask_to_mesh_assets(mask, elem)
-        assets = replace(assets, pixel_data=build_pixel_assets(mesh, ref, 1.0, assets.roi_mask))
-        out.append(Workload(f"seq{s}_{H}px_e{elem}", ref, frames, mask, mesh, assets,
-                            MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1),
-                            InitMotionConfig(win=17, search=8, score_min=0.2), warps))
-    return out
+        specs.append((s, H, elem, ref, frames, ellipse_mask(H, H, r), warps))
+    built = _build_assets([(sp[5], sp[3]) for sp in specs], [sp[2] for sp in specs])
+    return [Workload(f"seq{s}_{H}px_e{elem}", ref, frames, mask, mesh, assets,
+                     MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1),
+                     InitMotionConfig(win=17, search=8, score_min=0.2), warps)
+            for (s, H, elem, ref, frames, mask, warps), (mesh, assets) in zip(specs, built)]
 
 
 def plate_hole_2048(n_frames: int = 20, seed: int = 1, device="cpu", H: int = 2048) -> Workload:
@@ -107,3 +122,51 @@ def plate_hole_2048(n_frames: int = 20, seed: int = 1, device="cpu", H: int = 20
     return Workload("plate_hole_2048" if H == 2048 else f"plate_hole_{H}", ref, frames, mask, mesh, assets,
                     MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1),
                     InitMotionConfig(win=17, search=8, score_min=0.2), warps)
+
+
+def uneven_batch(n_frames: int = 64, seed: int = 2, device="cpu", sides=(512, 1024, 2048, 3072, 4096),
+                 elements=(8, 12, 16, 24, 32)):
+    """Independent frames of uneven size for one batched launch (frame i uses seed ``2000 + i``).
+
+    Per frame: side and element size drawn uniformly, ellipse mask covering
+    40-90%, a random affine map (strains +-2%, rotation +-1 deg, translation
+    +-3 px) about the image centre, N(0, 0.5^2) grey noise on both images.
+    """
+    import math
+    from dataclasses import replace
+
+    from .synthetic import Affine, ellipse_mask
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_frames):
+        H = int(rng.choice(sides))
+        elem = int(rng.choice(elements))
+        r = np.random.default_rng(2000 + i)
+        exx, eyy, exy = r.uniform(-0.02, 0.02, 3)
+        th = math.radians(r.uniform(-1.0, 1.0))
+        t = r.uniform(-3.0, 3.0, 2)
+        A = np.array([[exx, exy], [exy, eyy]]) + np.array([[math.cos(th) - 1, -math.sin(th)],
+                                                          [math.sin(th), math.cos(th) - 1]])
+        warp = Affine(A, t, [H / 2, H / 2])
+        ref, frames = speckle_sequence(H, H, [warp], seed=2000 + i, noise_seeds=[20000 + 2 * i, 20001 + 2 * i],
+                                       noise_sigma=0.5, device=device)
+        specs.append((i, H, elem, ref, frames, ellipse_mask(H, H, r), warp))
+    built = _build_assets([(sp[5], sp[3]) for sp in specs], [sp[2] for sp in specs])
+    return [Workload(f"frame{i}_{H}px_e{elem}", ref, frames, mask, mesh, assets,
+                     MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1), None, [warp])
+            for (i, H, elem, ref, frames, mask, warp), (mesh, assets) in zip(specs, built)]
+
+
+def uniaxial_1024(seed: int = 3, device="cpu") -> Workload:
+    """1024^2 speckle, centred 900^2 mask, 12 px elements, uniform 0.5% uniaxial strain (x)."""
+    from dataclasses import replace
+
+    from .synthetic import Affine
+    H = W = 1024
+    warp = Affine(np.array([[0.005, 0.0], [0.0, 0.0]]), np.zeros(2), [H / 2, W / 2])
+    ref, frames = speckle_sequence(H, W, [warp], seed=seed, noise_seeds=[seed, seed + 1], device=device)
+    mask = rect_mask(H, W, 900, 900)
+    mesh, assets = mask_to_mesh_assets(mask, 12)
+    assets = replace(assets, pixel_data=build_pixel_assets(mesh, ref, 1.0, assets.roi_mask))
+    return Workload("uniaxial_1024", ref, frames, mask, mesh, assets,
+                    MeshDICConfig(max_iters=400, tol=1e-5, reg_strength=0.1), None, [warp])
