@@ -26,6 +26,7 @@ from .batch_mesh_based import BatchBase, BatchMeshBased
 from .propagators import DisplacementPropagatorBase, PreviousDisplacementPropagator, ConstantVelocityPropagator
 from .solver_translation_zncc import TranslationZNCCSolver
 from .solver_global_cg import GlobalCGSolver
+from .solver_local_gn import LocalGaussNewtonSolver, LocalGNResult
 
 __all__ = [
     "Array", "InitMotionConfig", "MeshDICConfig", "DICResult", "DICDiagnostics", "BatchConfig", "BatchResult",
@@ -34,5 +35,5 @@ __all__ = [
     "build_pixel_assets", "compute_green_lagrange_strain_nodes_lsq", "green_lagrange_to_voigt",
     "small_strain_nodes_lsq", "SolverBase", "DICBase", "DICInitMotion", "DICMeshBased", "BatchBase",
     "BatchMeshBased", "DisplacementPropagatorBase", "PreviousDisplacementPropagator", "ConstantVelocityPropagator",
-    "TranslationZNCCSolver", "GlobalCGSolver",
+    "TranslationZNCCSolver", "GlobalCGSolver", "LocalGaussNewtonSolver", "LocalGNResult",
 ]

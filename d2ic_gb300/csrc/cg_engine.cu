@@ -385,23 +385,15 @@ __device__ __forceinline__ int tile_origin(int box0, const float ux[4], const fl
     return (ox & 0xffff) | (int)((unsigned)oy << 16);
 }
 
-// Release increment of a completion counter: the calling thread's earlier writes, and those of
-// the lanes it synchronised with (__syncwarp), are visible before the count.
-__device__ __forceinline__ void red_release_add(int *p, int v) {
-    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ int atom_acq_rel_add(int *p, int v) {
     int old;
     asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
     return old;
 }
 
-// `sig` (lanes 0..3): the group counter the previous chunk of this warp still has to count
-// (deferred so that its slot stores are long complete when the release is issued); on
-// return, this chunk's.
 template <int KIND>
 __device__ __forceinline__ void chunk_compute(const d2ic_frame_t &F, const ChunkMeta &m, float2 uc, const Stage &st,
-                                              const uint4 *srec, const float *tile, int lane, int *&sig) {
+                                              const uint4 *srec, const float *tile, int lane) {
     const bool staged = st.staged;
     const bool tiled = KIND == D2IC_INTERP_CUBIC && st.tiled;
     const int tw = F.tile_w, th = F.tile_h, tx0 = st.tx0, ty0 = st.ty0;
@@ -460,7 +452,6 @@ __device__ __forceinline__ void chunk_compute(const d2ic_frame_t &F, const Chunk
         gya[a] = warp_sum_f(gya[a]);
     }
     if (lane == 0 && tw > 0) F.chunk_tile[m.c] = tile_origin(m.box0, ux, uy);
-    if (sig) red_release_add(sig, 1);              // the previous chunk's counts (its slots are old)
     // lane a stores node a's partial in the chunk's slot of that node; node 0's slot also
     // carries the chunk's sum of r^2 (double-float), so every chunk is counted exactly once
     if (lane < 4) {
@@ -469,15 +460,18 @@ __device__ __forceinline__ void chunk_compute(const d2ic_frame_t &F, const Chunk
         reinterpret_cast<float4 *>(F.node_grad)[(size_t)m.slot * F.n_nodes + m.nd] =
             make_float4(gx, gy, lane == 0 ? js.hi : 0.f, lane == 0 ? js.lo : 0.f);
     }
-    // one count per distinct node group of the chunk (the group's reducer waits for all of them),
-    // issued by the lane holding the group's first node after the next chunk or the pixel pass ends
-    const int grp = m.nd / GN;
+    __syncwarp();                                   // every lane is done with the staged buffers
+}
+
+// One count per distinct node group among a chunk's four nodes (lanes 0..3 hold the node
+// indices); the group's reducer waits until it has as many counts as chunks touch the group.
+__device__ __forceinline__ void count_chunk_groups(int *group_cnt, int nd, int lane) {
+    const int grp = nd / GN;
     const int g0 = __shfl_sync(0xffffffffu, grp, 0), g1 = __shfl_sync(0xffffffffu, grp, 1),
               g2 = __shfl_sync(0xffffffffu, grp, 2);
     const bool first = lane == 0 || (lane == 1 && grp != g0) || (lane == 2 && grp != g0 && grp != g1) ||
                        (lane == 3 && grp != g0 && grp != g1 && grp != g2);
-    sig = (lane < 4 && first) ? F.group_cnt + grp : nullptr;
-    __syncwarp();                                   // every lane is done with the staged buffers
+    if (lane < 4 && first) atomicAdd(group_cnt + grp, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -927,7 +921,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             ChunkMeta m0{}, m1{}, m2{};
             CandRaw r0{}, r1{};
             Stage st0{}, st1{};
-            int *sig = nullptr;   // deferred group count of the warp's previous chunk (lanes 0..3)
+            bool p_ok = true;
             if (gw < total) {
                 m0 = fetch_meta(gw);
                 st0 = issue(m0, pipe_i, r0);
@@ -944,6 +938,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                         atomicExch(&C.h->abort, 1);
                     }
                     if (has1) mbar_wait(&s_bar[wid][(pipe_i + 1) & 1], ((pipe_i + 1) >> 1) & 1u);   // bounded
+                    p_ok = false;
                     break;
                 }
                 float2 uc = make_float2(0.f, 0.f);
@@ -955,14 +950,35 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 chunk_compute<KIND>(frames[m0.f], m0, uc, st0,
                                     reinterpret_cast<const uint4 *>(wbuf + (pipe_i & 1) * CHUNK_BYTES),
                                     reinterpret_cast<const float *>(wbuf + 2 * CHUNK_BYTES + (pipe_i & 1) * TILE_BYTES),
-                                    lane, sig);
+                                    lane);
                 ++pipe_i;
                 m0 = m1;
                 r0 = r1;
                 st0 = st1;
                 m1 = m2;
             }
-            if (sig) red_release_add(sig, 1);          // the last chunk's counts
+            // ---- count this warp's chunks into their node groups: one fence for the whole pass
+            // (a fence per chunk would also wait for the pipeline's prefetch loads in flight) ----
+            __threadfence();
+            __syncwarp();
+            if (p_ok) {
+                cur = 0;
+                for (int g = gw; g < total; g += nw) {
+                    int f, base;
+                    if (cached) {
+                        while (cur + 1 < na && s_cpre[cur + 1] <= g) ++cur;
+                        f = s_act[cur];
+                        base = s_cpre[cur];
+                    } else {
+                        const int s = find_slot(C.cpre, na, g);
+                        f = __ldcg(C.active + s);
+                        base = __ldcg(C.cpre + s);
+                    }
+                    const d2ic_frame_t &F = frames[f];
+                    const int nd = lane < 4 ? __ldg(F.chunk_nodes + 4 * (g - base) + lane) : 0;
+                    count_chunk_groups(F.group_cnt, nd, lane);
+                }
+            }
             if (trr) trace[7 * round + 1] = gtimer();
             // ---- N work: group gi of the active list goes to global warp gi mod (warps in grid); the
             // warp waits until every chunk with a node in the group has written its slots ----

@@ -37,6 +37,7 @@ class DICMeshBased(DICBase):
         self.config = config
         self._state: MeshDICState | None = None
         self._strain_dev = None
+        self._map_layout = None
 
     def prepare(self, ref_image: Array, assets: Optional[MeshAssets] = None) -> None:
         if assets is None:
@@ -52,6 +53,7 @@ class DICMeshBased(DICBase):
         self._state = MeshDICState(ref_image=ref, nodes_xy_device=np.asarray(assets.mesh.nodes_xy, dtype=np.float32),
                                    assets=assets, config=self.config, u0_nodal=None)
         self._strain_dev = None
+        self._map_layout = None
         self.solver.compile(assets)
         if hasattr(self.solver, "warmup"):
             self.solver.warmup(self._state)
@@ -103,7 +105,30 @@ class DICMeshBased(DICBase):
         else:
             strain = np.zeros((np.asarray(u_nodal).shape[0], 3), dtype=np.float32)
             info["strain"] = "skipped_no_neighbors"
+        pixel_maps = {}
         if bool(getattr(self.config, "compute_discrepancy_map", False)):
-            info["discrepancy"] = "unsupported"
+            if assets.pixel_data is None:
+                info["discrepancy"] = "skipped_no_pixel_assets"
+            else:
+                u_src = getattr(sol, "u_device", None)
+                dmap, rms = self._discrepancy(def_image, u_src if u_src is not None else u_nodal)
+                pixel_maps["discrepancy_ref"] = dmap        # kept on the device, as the reference keeps it
+                info["discrepancy"] = "discrepancy_ref"
+                info["discrepancy_rms"] = rms
         return DICResult(u_nodal=u_nodal, strain=strain, diagnostics=DICDiagnostics(info=info),
-                         history=getattr(sol, "history", None), pixel_maps={})
+                         history=getattr(sol, "history", None), pixel_maps=pixel_maps)
+
+    def _discrepancy(self, def_image, u):
+        """Discrepancy map through the solver's device layout (or one built for the maps)."""
+        from .engine import FrameSlot, descriptors_to_device
+        from .pixel_maps import discrepancy_map_ref
+        layout = getattr(self.solver, "_layout", None)
+        desc = getattr(self.solver, "_desc_dev", None)
+        if layout is None or desc is None:
+            if self._map_layout is None:
+                from .engine import FrameLayout
+                n_nodes = int(np.asarray(self._state.assets.mesh.nodes_xy).shape[0])
+                lay = FrameLayout(self._state.assets.pixel_data, n_nodes, self._state.ref_image, "linear")
+                self._map_layout = (lay, descriptors_to_device([FrameSlot(lay, 1).desc], lay.device))
+            layout, desc = self._map_layout
+        return discrepancy_map_ref(layout, desc, def_image, u)

@@ -148,6 +148,41 @@ D2IC_API int d2ic_pack_pixels(const int *colrow, const float *xieta, int n,
                      const float *coeff1, int H, int W, int pad, int cpitch, int kind,
                      d2ic_pixrec_t *out, void *stream);
 
+/* ---- local Gauss-Newton refinement (replaces LocalGaussNewtonSolver,
+ *      d2ic/solver_local_gn.py:34-414) ---- */
+
+/* Central-difference gradient images of an HxW image, zero on the first/last
+ * column (gx) and row (gy) (_compute_image_gradient_jax, :204-210). */
+D2IC_API int d2ic_central_gradient(const float *img, int H, int W, float *gx, float *gy, void *stream);
+
+/* Bytes of the per-node slot scratch of one sweep (zero it once; unused slots must stay 0). */
+D2IC_API size_t d2ic_local_gn_slot_bytes(int n_nodes, int node_chunk_k);
+
+/* One Jacobi sweep u -> u_next (_local_sweeps body, :283-313; jacobi_nodal_step_spring,
+ * :316-414): frame_dev carries the deformed image's sampling array (coeff) and the
+ * pixel/chunk layout; coeff_gx/coeff_gy the gradient images' sampling arrays in the
+ * same layout; has_pix: 1 for nodes with pixels; nbr_index/nbr_weight: raw spring
+ * table (max_deg x n_nodes, column-major, -1 after the last neighbour);
+ * node_reg_weight: rho_i.  chunk_r2 (n_chunks doubles) and step_part (one double
+ * per 256 nodes) receive the sums for the sweep's RMS history. */
+D2IC_API int d2ic_local_gn_sweep(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
+                                 int interp_kind, const float *coeff_gx, const float *coeff_gy, const float *u,
+                                 float *slots, double *chunk_r2, const int *has_pix, const int *nbr_index,
+                                 const float *nbr_weight, int max_deg, const float *node_reg_weight, float lam,
+                                 float max_step, float alpha_reg, float omega, float *u_next, double *step_part,
+                                 void *stream);
+
+/* ---- result maps (replaces compute_discrepancy_map_ref, d2ic/discrepancy.py:86-127) ---- */
+
+/* Bilinear grey-level residual I_def(x + u(x)) - I_ref(x) at every ROI pixel of
+ * the frame's pixel list, written at (row, col) of the HxW `map` (NaN elsewhere
+ * and where the bilinear stencil leaves the image), with per-chunk FP64 sums of
+ * r^2 and valid counts for the RMS.  frame_dev: device descriptor (pix,
+ * chunk_begin, chunk_nodes, n_chunks, W, H); ref, def: HxW images; u: 2 * n_nodes. */
+D2IC_API int d2ic_discrepancy_map(const d2ic_frame_t *frame_dev, int n_chunks, const float *ref, const float *def,
+                                  const float *u, int H, int W, float *map, double *chunk_sums, int *chunk_counts,
+                                  void *stream);
+
 /* ---- global CG engine (replaces _cg_solve / _J_TOTAL_VG / J_total,
  *      d2ic/solver_global_cg.py:289-469, behind GlobalCGSolver.solve :151-198) ---- */
 

@@ -12,7 +12,8 @@ def _frame(H=128, elem=16, seed=5):
     import d2ic_gb300 as d2
     from d2ic_gb300.synthetic import Translation, rect_mask, speckle_sequence
     ref, frames = speckle_sequence(H, H, [Translation(0.4, -0.3)], seed=seed, noise_seeds=[seed, seed + 1])
-    mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, H, H - 16, H - 16), elem)
+    # ROI on the element grid (16..112): every element lies inside it, no weakly held corner nodes
+    mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, H, H - 32, H - 32), elem)
     pix = d2.build_pixel_assets(mesh, ref, 1.0, assets.roi_mask)
     return ref, frames[0], mesh, assets, pix
 
@@ -42,9 +43,7 @@ def test_tuned_solve_matches_oracle(cuda):
     ref, deformed, mesh, assets, pix = _frame()
     from dataclasses import replace
     assets = replace(assets, pixel_data=pix)
-    # converged tightly on both sides: weakly constrained corner nodes otherwise keep CG-path
-    # differences far above the tolerance whatever the launch shape
-    cfg = d2.MeshDICConfig(max_iters=1000, tol=1e-6, reg_strength=0.1)
+    cfg = d2.MeshDICConfig(max_iters=1000, tol=1e-5, reg_strength=0.1)
     solver = d2.GlobalCGSolver(device=cuda, autotune=True)
     dic = d2.DICMeshBased(mesh, solver, cfg)
     dic.prepare(ref, assets)
@@ -57,6 +56,6 @@ def test_tuned_solve_matches_oracle(cuda):
     from oracle import objective, pixels
     oa = pixels.build_pixel_assets(np.asarray(mesh.nodes_xy), np.asarray(mesh.elements), 128, 128, assets.roi_mask)
     pb = objective.Problem.build(ref, deformed, oa)
-    u_ref, _, _, _ = fast.FastProblem(pb).cg_solve(np.zeros((mesh.nodes_xy.shape[0], 2)), 0.1, 1000, 1e-6)
+    u_ref, _, _, _ = fast.FastProblem(pb).cg_solve(np.zeros((mesh.nodes_xy.shape[0], 2)), 0.1, 1000, 1e-5)
     used = np.unique(np.asarray(mesh.elements))
     assert np.abs(np.asarray(res.u_nodal, np.float64)[used] - u_ref[used]).max() <= 1e-3

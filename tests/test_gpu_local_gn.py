@@ -1,0 +1,60 @@
+"""Local Gauss-Newton refinement (d2ic/solver_local_gn.py) on the GPU vs the FP64 oracle sweeps."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(interp):
+    from dataclasses import replace
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300.synthetic import Affine, rect_mask, speckle_sequence
+    H = 128
+    ref, frames = speckle_sequence(H, H, [Affine([[0.004, 0.001], [0.0, -0.003]], [0.45, -0.3], [64, 64])], seed=12,
+                                   noise_seeds=[12, 13])
+    mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, H, 112, 112), 16)
+    assets = replace(assets, pixel_data=d2.build_pixel_assets(mesh, ref, 1.0, assets.roi_mask))
+    return ref, frames[0], mesh, assets
+
+
+@pytest.mark.parametrize("interp", ["cubic", "linear"])
+def test_local_gn_sweeps_match_oracle(cuda, interp):
+    import d2ic_gb300 as d2
+    from oracle import local_gn, objective, pixels
+    ref, deformed, mesh, assets = _case(interp)
+    n_sweeps = 6
+    cfg = d2.MeshDICConfig(max_iters=n_sweeps, tol=1e-3, reg_strength=0.1, save_history=True)
+    dic = d2.DICMeshBased(mesh, d2.LocalGaussNewtonSolver(lam=1e-3, max_step=0.2, omega=0.5, interpolation=interp,
+                                                          device=cuda), cfg)
+    dic.prepare(ref, assets)
+    u0 = np.tile(np.array([[0.4, -0.25]], np.float32), (mesh.nodes_xy.shape[0], 1))
+    dic.set_initial_guess(u0)
+    res = dic.run(deformed)
+    oa = pixels.build_pixel_assets(np.asarray(mesh.nodes_xy), np.asarray(mesh.elements), 128, 128, assets.roi_mask)
+    pb = objective.Problem.build(ref, deformed, oa, interpolation=interp)
+    u_ref, h_ref = local_gn.local_sweeps(u0, pb, 1e-3, 0.2, 0.1, 0.5, n_sweeps)
+    err = np.abs(np.asarray(res.u_nodal, np.float64) - u_ref).max()
+    assert err <= 1e-3, err                                          # nodal tolerance, px
+    hist = np.asarray(res.history)
+    assert hist.shape == (n_sweeps, 2)
+    assert np.allclose(hist, h_ref, rtol=1e-3, atol=1e-6)            # [rms r, rms step] per sweep
+
+
+def test_cg_then_local_chain(cuda):
+    """BatchMeshBased(dic_local=...): CG, then local sweeps from the CG solution (the reference pipeline)."""
+    import d2ic_gb300 as d2
+    ref, deformed, mesh, assets = _case("cubic")
+    cg = d2.DICMeshBased(mesh, d2.GlobalCGSolver(device=cuda), d2.MeshDICConfig(max_iters=200, tol=1e-3,
+                                                                                reg_strength=0.1))
+    loc = d2.DICMeshBased(mesh, d2.LocalGaussNewtonSolver(device=cuda), d2.MeshDICConfig(max_iters=3, tol=1e-3,
+                                                                                         reg_strength=0.1))
+    batch = d2.BatchMeshBased(ref, assets, cg, d2.BatchConfig(warm_start_from_previous=True), dic_local=loc)
+    batch.before([deformed])
+    out = batch.sequence([deformed])
+    u_cg = cg.run(deformed).u_nodal
+    u = np.asarray(out.results[0].u_nodal)
+    assert np.isfinite(u).all()
+    assert 0 < np.abs(u - np.asarray(u_cg)).max() < 0.2                 # a few relaxed local steps from CG
