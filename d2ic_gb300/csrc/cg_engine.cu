@@ -75,10 +75,11 @@ struct CtlHeader {
     int n_active;
     int total_chunks;
     int total_groups;
-    int rounds;
-    int finished;   // a frame finished in this round: the active list is rebuilt at the barrier
+    unsigned rounds_done;   // rounds completed in this launch (released by the round's last frame step)
+    int finished;           // a frame finished in this round: the active list is rebuilt before release
     int max_rounds;
-    int pad_[6];
+    int frames_done;        // frames whose control step ran in the current round
+    int pad_[5];
 };
 
 struct Ctl {
@@ -746,6 +747,51 @@ __device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
 // node group: the group partials are summed in group order (double-float,
 // then FP64) and the frame state advanced.  Nothing else reads the frame's
 // state in this round once all its groups are reduced.
+// Active list rebuilt by one warp (the warp that ends a round): lane l scans a contiguous
+// block of frames, a warp scan gives each block its slot and prefix offsets.
+__device__ void rebuild_active_warp(const d2ic_frame_t *frames, int n_frames, Ctl &C, int lane) {
+    const int per = (n_frames + 31) / 32;
+    const int f0 = min(lane * per, n_frames), f1 = min(f0 + per, n_frames);
+    int cnt = 0, ch = 0, gr = 0;
+    for (int f = f0; f < f1; ++f)
+        if (ld_vol(&C.fs[f].state) != ST_DONE) {
+            ++cnt;
+            ch += frames[f].n_chunks;
+            gr += frames[f].n_groups;
+        }
+    int ic = cnt, ih = ch, ig = gr;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(0xffffffffu, ic, o), b = __shfl_up_sync(0xffffffffu, ih, o),
+                  c = __shfl_up_sync(0xffffffffu, ig, o);
+        if (lane >= o) {
+            ic += a;
+            ih += b;
+            ig += c;
+        }
+    }
+    const int ta = __shfl_sync(0xffffffffu, ic, 31), tb = __shfl_sync(0xffffffffu, ih, 31),
+              tc = __shfl_sync(0xffffffffu, ig, 31);
+    int slot = ic - cnt, cp = ih - ch, gp = ig - gr;
+    for (int f = f0; f < f1; ++f)
+        if (ld_vol(&C.fs[f].state) != ST_DONE) {
+            C.active[slot] = f;
+            C.cpre[slot] = cp;
+            C.gpre[slot] = gp;
+            ++slot;
+            cp += frames[f].n_chunks;
+            gp += frames[f].n_groups;
+        }
+    if (lane == 0) {
+        C.h->n_active = ta;
+        C.h->total_chunks = tb;
+        C.h->total_groups = tc;
+        C.cpre[ta] = tb;
+        C.gpre[ta] = tc;
+    }
+    __syncwarp();
+}
+
 __device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int lane) {
     DF q[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     const int nsg = (F.n_groups + GN - 1) / GN;
@@ -1060,20 +1106,50 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                         const bool rt = trace != nullptr && lane == 0 && round < trace_rounds;
                         if (rt) trace[7 * round + 3] = gtimer();
                         frame_r(F, f, C, eval_only, lane);
+                        int last_frame = 0;
+                        if (lane == 0) last_frame = atom_acq_rel_add(&C.h->frames_done, 1) == na - 1;
+                        __syncwarp();
+                        if (__shfl_sync(0xffffffffu, last_frame, 0)) {
+                            // every frame of the round has run its control step, so every block's
+                            // work of the round is done: rebuild the active list and release the round
+                            if (lane == 0) C.h->frames_done = 0;
+                            if (ld_vol(&C.h->finished)) {
+                                rebuild_active_warp(frames, n_frames, C, lane);
+                                if (lane == 0) C.h->finished = 0;
+                            }
+                            __syncwarp();
+                            if (lane == 0) {
+                                __threadfence();
+                                atomicExch(&C.h->rounds_done, (unsigned)(round + 1));
+                            }
+                        }
                         if (rt) trace[7 * round + 4] = gtimer();
                     }
                 }
             }
             if (trr) trace[7 * round + 2] = gtimer();
         }
-        // ---- end of round: the last block to arrive rebuilds the active list if a frame finished ----
-        if (!grid_barrier(C.h, [&] {
-                if (ld_vol(&C.h->finished)) {
-                    rebuild_active(frames, n_frames, C);
-                    if (threadIdx.x == 0) C.h->finished = 0;
+        // ---- end of round: wait until the warp that ran the round's last frame step releases it
+        // (rounds_done is monotonic, so a block that arrives after the release passes at once) ----
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned target = (unsigned)(round + 1);
+            if (ld_acquire_u32(&C.h->rounds_done) < target) {
+                const unsigned long long t0 = gtimer();
+                while (ld_acquire_u32(&C.h->rounds_done) < target) {
+                    if (ld_vol(&C.h->abort)) break;
+                    if (gtimer() - t0 > WAIT_NS) {
+                        C.h->err = D2IC_WAIT_TIMEOUT;
+                        atomicExch(&C.h->abort, 1);
+                        break;
+                    }
+                    __nanosleep(64);
                 }
-            }))
-            break;
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        if (ld_vol(&C.h->abort)) break;
         if (trr) trace[7 * round + 5] = gtimer();
         ++round;
     }

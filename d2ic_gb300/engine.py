@@ -157,6 +157,27 @@ class FrameLayout:
             by1 = np.maximum.reduceat(colrow[:, 1], cstart)
             chunk_box = np.stack([bx0 | (by0 << 16), bx1 | (by1 << 16)], axis=1).astype(np.int64)
             chunk_box = chunk_box.astype(np.uint32).view(np.int32)
+            # Pixel order inside full 16-column chunks (h rows, h a multiple of 8): the two
+            # half-warps of each 32-pixel step read rows r and r + 4 instead of r and r + 1, so that
+            # with the 28-float tile pitch of such chunks their taps fall 16 banks apart.  Only the
+            # order of a chunk's partial sums changes.
+            lens_c = np.diff(chunk_begin).astype(np.int64)
+            w_c, h_c = bx1 - bx0 + 1, by1 - by0 + 1
+            full = (w_c == 16) & (h_c % 8 == 0) & (lens_c == 16 * h_c)
+            if self.kind == _lib.INTERP_CUBIC and full.any():
+                cid = np.repeat(np.arange(self.n_chunks), lens_c)
+                sel = full[cid]
+                r = colrow[sel, 1] - by0[cid[sel]]
+                c = colrow[sel, 0] - bx0[cid[sel]]
+                dest = cstart[cid[sel]] + 32 * ((r & 3) + ((r >> 3) << 2)) + 16 * ((r >> 2) & 1) + c
+                src = np.flatnonzero(sel)
+                if np.bincount(dest, minlength=Np).max(initial=0) > 1:
+                    raise AssertionError("pixel permutation inside chunks is not one-to-one")
+                new = order.copy()
+                new[dest] = order[src]
+                order = new
+                colrow = np.stack([np.floor(pc[:, 0] - 0.5), np.floor(pc[:, 1] - 0.5)],
+                                  axis=1).astype(np.int64)[order]
         else:
             chunk_box = np.zeros((0, 2), np.int32)
         # node gradient slots: the chunk's partial for its local node a goes to slot rank(chunk) of
