@@ -478,40 +478,28 @@ __device__ __forceinline__ void count_chunk_groups(int *group_cnt, int nd, int l
 // ---------------------------------------------------------------------------
 // N work: one group of GN = 32 nodes per warp (lane = node)
 // ---------------------------------------------------------------------------
-// Per node: gather its chunk partials from its K slots (slot order), add the
-// spring gradient over the neighbour table, write the trial gradient, trial
-// point and trial direction, and return the node's terms of sum r^2 (from the
-// slots), spring energy, g.g, g.(g - g_cur) and g_cur.dir in double-float.
-__device__ __forceinline__ void node_work(const d2ic_frame_t &F, const FInfo &fi, int g, int lane, DF q[5]) {
-#pragma unroll
-    for (int i = 0; i < 5; ++i) q[i] = DF{0.f, 0.f};
-    const int n = g * GN + lane;
-    if (n >= F.n_nodes) return;
+// Per node, in two parts.  node_pre needs nothing from this round's pixel pass (the
+// candidate point, the trial direction, the current gradient and the spring terms), so a
+// warp runs it before it waits for its group's chunks; node_post gathers the chunk
+// partials from the node's K slots (slot order), writes the trial gradient, point and
+// direction, and returns the node's terms of sum r^2, spring energy, g.g, g.(g - g_cur)
+// and g_cur.dir in double-float.
+struct NodePre {
+    float2 ui, dir, gc;
+    float rx, ry, en;
+};
+
+__device__ __forceinline__ NodePre node_pre(const d2ic_frame_t &F, const FInfo &fi, int n) {
+    NodePre p;
+    p.rx = p.ry = p.en = 0.f;
+    p.ui = p.dir = p.gc = make_float2(0.f, 0.f);
+    if (n >= F.n_nodes) return p;
     const Cand cd = make_cand(F, fi);
-    // All loads of a batch are issued before any is consumed: the node pass is a short
-    // chain of L2 round trips instead of one per table entry.  Sums still run in table order.
-    const float2 gc = __ldcg(nbuf(F, 2 + fi.igc) + n);   // issued with the candidate's own loads
-    float2 dir;
-    const float2 ui = cd.at(n, dir);
-    float sx = 0.f, sy = 0.f;
-    DF sj = {0.f, 0.f};
-    const int K = F.node_chunk_k, Nn = F.n_nodes;
-    const float4 *ng = reinterpret_cast<const float4 *>(F.node_grad) + n;
-    constexpr int NB = 4;
-    for (int kb = 0; kb < K; kb += NB) {
-        float4 v[NB];
-#pragma unroll
-        for (int t = 0; t < NB; ++t) v[t] = (kb + t < K) ? __ldcg(ng + (size_t)(kb + t) * Nn) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-        for (int t = 0; t < NB; ++t)
-            if (kb + t < K) {
-                sx += v[t].x;
-                sy += v[t].y;
-                sj = df_add(sj, DF{v[t].z, v[t].w});
-            }
-    }
-    float rx = 0.f, ry = 0.f, en = 0.f;
-    const int md = F.max_deg;
+    // All loads of a batch are issued before any is consumed: a short chain of L2 round
+    // trips instead of one per table entry.  Sums still run in table order.
+    p.gc = __ldcg(nbuf(F, 2 + fi.igc) + n);
+    p.ui = cd.at(n, p.dir);
+    const int md = F.max_deg, Nn = F.n_nodes;
     const int *nbi = F.nbr_index + n;             // column-major: entry k at k * n_nodes
     const float *nbw = F.nbr_weight + n;
     bool alive = true;                               // entries after the first -1 are padding
@@ -534,26 +522,50 @@ __device__ __forceinline__ void node_work(const d2ic_frame_t &F, const FInfo &fi
         for (int t = 0; t < NBN; ++t) {
             alive = alive && jj[t] >= 0;
             if (alive) {
-                const float ddx = ui.x - uj[t].x, ddy = ui.y - uj[t].y;
-                rx += ww[t] * ddx;
-                ry += ww[t] * ddy;
-                en += ww[t] * (ddx * ddx + ddy * ddy);
+                const float ddx = p.ui.x - uj[t].x, ddy = p.ui.y - uj[t].y;
+                p.rx += ww[t] * ddx;
+                p.ry += ww[t] * ddy;
+                p.en += ww[t] * (ddx * ddx + ddy * ddy);
             }
         }
     }
+    return p;
+}
+
+__device__ __forceinline__ void node_post(const d2ic_frame_t &F, const FInfo &fi, int n, const NodePre &p, DF q[5]) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) q[i] = DF{0.f, 0.f};
+    if (n >= F.n_nodes) return;
+    float sx = 0.f, sy = 0.f;
+    DF sj = {0.f, 0.f};
+    const int K = F.node_chunk_k, Nn = F.n_nodes;
+    const float4 *ng = reinterpret_cast<const float4 *>(F.node_grad) + n;
+    constexpr int NB = 4;
+    for (int kb = 0; kb < K; kb += NB) {
+        float4 v[NB];
+#pragma unroll
+        for (int t = 0; t < NB; ++t) v[t] = (kb + t < K) ? __ldcg(ng + (size_t)(kb + t) * Nn) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < NB; ++t)
+            if (kb + t < K) {
+                sx += v[t].x;
+                sy += v[t].y;
+                sj = df_add(sj, DF{v[t].z, v[t].w});
+            }
+    }
     const float inv_np = 1.0f / (float)max(F.n_pix, 1);
-    const float gx = sx * inv_np + F.alpha_reg * rx;
-    const float gy = sy * inv_np + F.alpha_reg * ry;
+    const float gx = sx * inv_np + F.alpha_reg * p.rx;
+    const float gy = sy * inv_np + F.alpha_reg * p.ry;
     nbuf(F, 2 + fi.igt)[n] = make_float2(gx, gy);
-    nbuf(F, 1 - fi.iu)[n] = ui;
-    nbuf(F, 5 + (1 - fi.idp))[n] = dir;
+    nbuf(F, 1 - fi.iu)[n] = p.ui;
+    nbuf(F, 5 + (1 - fi.idp))[n] = p.dir;
     // per-node terms of the inner products, exact in double-float (g - g_cur rounded
     // in FP32 as the reference's elementwise difference)
     q[P_JSUM] = sj;
-    q[P_EREG] = DF{0.25f * en, 0.f};
+    q[P_EREG] = DF{0.25f * p.en, 0.f};
     q[P_GG] = df_add(df_prod(gx, gx), df_prod(gy, gy));
-    q[P_GDIFF] = df_add(df_prod(gx, gx - gc.x), df_prod(gy, gy - gc.y));
-    q[P_GD] = df_add(df_prod(gc.x, dir.x), df_prod(gc.y, dir.y));
+    q[P_GDIFF] = df_add(df_prod(gx, gx - p.gc.x), df_prod(gy, gy - p.gc.y));
+    q[P_GD] = df_add(df_prod(p.gc.x, p.dir.x), df_prod(p.gc.y, p.dir.y));
 }
 
 // ---------------------------------------------------------------------------
@@ -794,6 +806,8 @@ __device__ void rebuild_active_warp(const d2ic_frame_t *frames, int n_frames, Ct
 
 __device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int lane) {
     DF q[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    FrameState S;
+    if (lane == 0) S = load_fs(C.fs + f);              // in flight with the partials below
     const int nsg = (F.n_groups + GN - 1) / GN;
     const float2 *sp = reinterpret_cast<const float2 *>(F.group_part) + (size_t)F.n_groups * D2IC_NPART;
     for (int g = lane; g < nsg; g += 32) {
@@ -806,7 +820,6 @@ __device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int
 #pragma unroll
     for (int i = 0; i < 5; ++i) q[i] = df_warp_sum(q[i]);
     if (lane == 0) {
-        FrameState S = load_fs(C.fs + f);
         double qd[5];
 #pragma unroll
         for (int i = 0; i < 5; ++i) qd[i] = df_to_double(q[i]);
@@ -1044,6 +1057,8 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 }
                 const d2ic_frame_t &F = frames[f];
                 const int g = gi - base;
+                const FInfo fi = cached ? s_fi[s] : frame_info(C.fs + f);
+                const NodePre pre = node_pre(F, fi, g * GN + lane);   // independent of the pixel pass
                 int ok = 1;
                 if (lane == 0) {
                     const int need = __ldg(F.group_need + g);
@@ -1067,9 +1082,8 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 }
                 __syncwarp();                          // the slots seen by lane 0 are seen by the warp
                 if (!__shfl_sync(0xffffffffu, ok, 0)) break;
-                const FInfo fi = cached ? s_fi[s] : frame_info(C.fs + f);
                 DF q[5];
-                node_work(F, fi, g, lane, q);
+                node_post(F, fi, g * GN + lane, pre, q);
 #pragma unroll
                 for (int i = 0; i < 5; ++i) q[i] = df_warp_sum(q[i]);
                 // group -> supergroup (32 groups) -> frame: the warp that completes a level reduces it
@@ -1107,7 +1121,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                         if (rt) trace[7 * round + 3] = gtimer();
                         frame_r(F, f, C, eval_only, lane);
                         int last_frame = 0;
-                        if (lane == 0) last_frame = atom_acq_rel_add(&C.h->frames_done, 1) == na - 1;
+                        if (lane == 0) last_frame = na == 1 || atom_acq_rel_add(&C.h->frames_done, 1) == na - 1;
                         __syncwarp();
                         if (__shfl_sync(0xffffffffu, last_frame, 0)) {
                             // every frame of the round has run its control step, so every block's
