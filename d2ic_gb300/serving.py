@@ -17,6 +17,12 @@ and mesh sizes are served at once:
   at the next slice (continuous batching: work of requests that arrive while
   others are on the GPU overlaps on the device);
 * the slice launch is captured once in a CUDA graph and replayed;
+* host work overlaps the device: while slice k runs, the host harvests slice
+  k-1 (status copied back asynchronously into pinned memory), queues the
+  finished frames' strain kernels and result copies (pinned, completed by
+  event polling), admits new requests and queues slice k+1 behind slice k;
+* each sequence owns one device slot (coefficients, node buffers, workspace)
+  reused by its frames, so admission allocates nothing;
 * frames of one sequence are solved in order (frame k+1 starts from frame k's
   solution, as BatchMeshBased with warm_start_from_previous), so a frame's
   result is the same whether it is solved alone or in the mix: every reduction
@@ -92,6 +98,10 @@ class _Sequence:
     in_flight: bool = False
     queue: collections.deque = field(default_factory=collections.deque)
     frames_done: int = 0
+    slot: Any = None                     # the sequence's device slot, reused by its frames
+    centers_dev: Any = None
+    out_u: Any = None                    # pinned result buffers
+    out_strain: Any = None
 
 
 class DICServer:
@@ -112,7 +122,12 @@ class DICServer:
         self.desc_dev = torch.zeros(S * nb, dtype=torch.uint8, device=self.device)
         self.slots: list[tuple[FrameSlot, Request, _Sequence] | None] = [None] * S
         self.status_dev = torch.zeros((S, 3), dtype=torch.int32, device=self.device)   # n_iters, status, n_evals
-        self.status_host = torch.zeros((S, 3), dtype=torch.int32).pin_memory()
+        self.status_host = [torch.zeros((S, 3), dtype=torch.int32).pin_memory() for _ in range(2)]
+        self.status_event = [torch.cuda.Event(), torch.cuda.Event()]
+        self.desc_host = torch.zeros(S * nb, dtype=torch.uint8).pin_memory()
+        self.pending_slices: collections.deque = collections.deque()   # parities of slices not harvested
+        self.parity = 0
+        self.awaiting: list = []                                       # (request, sequence, event)
         self.seqs: dict[Any, _Sequence] = {}
         self.ready: collections.deque = collections.deque()     # sequences with queued frames, FIFO
         self.completed: list[Request] = []
@@ -178,8 +193,9 @@ class DICServer:
 
     def reset_sequences(self):
         """Forget warm starts and completed requests (resident layouts are kept)."""
-        if any(x is not None for x in self.slots):
+        if any(x is not None for x in self.slots) or self.pending_slices:
             raise RuntimeError("reset while frames are in flight")
+        self._complete(wait=True)
         for s in self.seqs.values():
             s.u_prev = None
             s.queue.clear()
@@ -193,16 +209,17 @@ class DICServer:
         t0 = time.perf_counter()
         i = 0
         n = len(requests)
-        while i < n or self.pending():
+        while i < n or self.pending() or self.pending_slices:
             now = time.perf_counter() - t0
             while i < n and offsets[i] <= now:
                 requests[i].t_arrival = t0 + offsets[i]
                 self.submit(requests[i])
                 i += 1
-            if self.pending():
+            if self.pending() or self.pending_slices:
                 self.step()
             elif i < n:
                 time.sleep(max(0.0, offsets[i] - (time.perf_counter() - t0)))
+        self._complete(wait=True)
         return self.completed
 
     def pending(self) -> int:
@@ -212,17 +229,26 @@ class DICServer:
     def _admit(self):
         free_slots = [i for i, x in enumerate(self.slots) if x is None]
         admitted = 0
+        stream = torch.cuda.current_stream(self.device)
+        nb = _desc_bytes()
         while free_slots and self.ready:
             seq = self.ready[0]
             L = seq.layout
-            need = self._slot_bytes(L, seq.config.max_iters)
-            if self.bytes_in_use + need > self.budget:
-                break                                       # wait for memory to free up
+            if seq.slot is None:                             # first frame: the sequence's resident slot
+                need = self._slot_bytes(L, seq.config.max_iters)
+                if self.bytes_in_use + need > self.budget:
+                    break                                    # wait for memory to free up
+                seq.slot = FrameSlot(L, seq.config.max_iters)
+                seq.slot.set_params(seq.config.tol, seq.config.reg_strength)
+                seq.out_u = torch.empty((L.n_nodes, 2), dtype=torch.float32).pin_memory()
+                seq.out_strain = torch.empty((L.n_nodes, 3), dtype=torch.float32).pin_memory()
+                if seq.centers is not None:
+                    seq.centers_dev = torch.as_tensor(seq.centers, device=self.device).reshape(-1, 2).contiguous()
+                self.bytes_in_use += need
             self.ready.popleft()
             req = seq.queue.popleft()
             i = free_slots.pop(0)
-            slot = FrameSlot(L, seq.config.max_iters)
-            slot.set_params(seq.config.tol, seq.config.reg_strength)
+            slot = seq.slot
             # image: pinned host -> device on the copy stream, then coefficients on the compute stream
             if isinstance(req.image, torch.Tensor) and req.image.is_cuda:
                 img = req.image.to(torch.float32)
@@ -232,30 +258,31 @@ class DICServer:
                 img = torch.empty((L.H, L.W), dtype=torch.float32, device=self.device)
                 with torch.cuda.stream(self.copy_stream):
                     img.copy_(src, non_blocking=True)
-                torch.cuda.current_stream(self.device).wait_stream(self.copy_stream)
-                img.record_stream(torch.cuda.current_stream(self.device))
+                stream.wait_stream(self.copy_stream)
+                img.record_stream(stream)
             slot.load_image(img)
             if seq.u_prev is not None:
                 slot.u0.copy_(seq.u_prev)
             elif seq.init is not None:                      # first frame: ZNCC at centres + IDW, on the device
                 from .dic_init_motion import project_centers_to_nodes_idw_device
                 from .solver_translation_zncc import match_centers_device
-                u_c, s = match_centers_device(seq.centers, L.ref_image, img, seq.init.win, seq.init.search, self.device)
+                u_c, sc = match_centers_device(seq.centers_dev, L.ref_image, img, seq.init.win, seq.init.search,
+                                               self.device)
                 if seq.init.score_min is not None:
-                    u_c = torch.where((s >= float(seq.init.score_min))[:, None], u_c, torch.zeros_like(u_c))
-                slot.u0.copy_(project_centers_to_nodes_idw_device(seq.nodes, seq.centers, u_c, 2.0, self.device))
+                    u_c = torch.where((sc >= float(seq.init.score_min))[:, None], u_c, torch.zeros_like(u_c))
+                slot.u0.copy_(project_centers_to_nodes_idw_device(seq.nodes, seq.centers_dev, u_c, 2.0, self.device))
             else:
                 slot.u0.zero_()
             # per-slot status words live in one array that is copied back after every slice
             slot.desc.n_iters = ptr(self.status_dev[i])
             slot.desc.status = ptr(self.status_dev[i]) + 4
             slot.desc.n_evals = ptr(self.status_dev[i]) + 8
-            nb = _desc_bytes()
-            self.desc_dev[i * nb:(i + 1) * nb].copy_(torch.frombuffer(bytearray(bytes(slot.desc)), dtype=torch.uint8))
+            hb = self.desc_host[i * nb:(i + 1) * nb]
+            hb.copy_(torch.frombuffer(bytearray(bytes(slot.desc)), dtype=torch.uint8))
+            self.desc_dev[i * nb:(i + 1) * nb].copy_(hb, non_blocking=True)
             self.cmd[i] = _lib.CMD_INIT
             self.status_dev[i, 1] = _lib.RUNNING
-            self.slots[i] = (slot, req, seq)
-            self.bytes_in_use += need
+            self.slots[i] = (slot, req, seq, self.slices)    # first slice that sees the frame
             seq.in_flight = True
             req.t_admit = time.perf_counter()
             admitted += 1
@@ -284,31 +311,33 @@ class DICServer:
         else:
             launch()
 
-    def _harvest(self):
-        self.status_host.copy_(self.status_dev, non_blocking=True)
-        torch.cuda.current_stream(self.device).synchronize()
-        now = time.perf_counter()
+    def _harvest(self, parity: int, slice_no: int):
+        """Frames that finished by slice ``slice_no`` (status copy of parity ``parity``)."""
+        self.status_event[parity].synchronize()
+        status = self.status_host[parity]
         done = 0
         for i, entry in enumerate(self.slots):
-            if entry is None:
+            if entry is None or entry[3] > slice_no:        # admitted after that slice was queued
                 continue
-            n_iters, st, _ = (int(x) for x in self.status_host[i])
+            n_iters, st, _ = (int(x) for x in status[i])
             if st == _lib.RUNNING:
                 continue
-            slot, req, seq = entry
+            slot, req, seq, _ = entry
             u = slot.u_out
             voigt, _ = strain_device(u, seq.nodes, seq.strain_idx, seq.strain_deg, seq.config.strain_gauge_length,
                                      seq.config.strain_eps, self.device)
-            seq.u_prev = u.clone()
-            req.u = u.cpu().numpy()
-            req.strain = voigt.cpu().numpy()
+            if seq.u_prev is None:
+                seq.u_prev = torch.empty_like(u)
+            seq.u_prev.copy_(u)
+            seq.out_u.copy_(u, non_blocking=True)
+            seq.out_strain.copy_(voigt, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record()
             req.n_iters = n_iters
             req.status = _lib.STATUS_NAMES.get(st, str(st))
-            req.t_done = now
-            self.completed.append(req)
+            self.awaiting.append((req, seq, ev))
             self.slots[i] = None
             self.cmd[i] = _lib.CMD_IDLE
-            self.bytes_in_use -= self._slot_bytes(seq.layout, seq.config.max_iters)
             seq.in_flight = False
             seq.frames_done += 1
             if seq.queue:
@@ -316,21 +345,49 @@ class DICServer:
             done += 1
         return done
 
+    def _complete(self, wait: bool = False):
+        """Requests whose result copies have landed in pinned memory."""
+        keep = []
+        for req, seq, ev in self.awaiting:
+            if wait or ev.query():
+                ev.synchronize()
+                req.u = seq.out_u.numpy().copy()
+                req.strain = seq.out_strain.numpy().copy()
+                req.t_done = time.perf_counter()
+                self.completed.append(req)
+            else:
+                keep.append((req, seq, ev))
+        self.awaiting = keep
+
     def step(self) -> int:
-        """Admit what fits, run one engine slice, harvest finished frames; returns frames completed."""
+        """Admit what fits, queue one engine slice, harvest the previous one; returns frames finished."""
         self._admit()
-        if all(x is None for x in self.slots):
-            return 0
+        done = 0
         t0 = time.perf_counter()
-        self._launch_slice()                        # the kernel turns CMD_INIT into CMD_RUN as it admits
-        done = self._harvest()
+        if any(x is not None for x in self.slots):
+            self._launch_slice()                    # the kernel turns CMD_INIT into CMD_RUN as it admits
+            p = self.parity
+            self.status_host[p].copy_(self.status_dev, non_blocking=True)
+            self.status_event[p].record()
+            self.pending_slices.append((p, self.slices))
+            self.parity ^= 1
+            self.slices += 1
+        # harvest the older slice while the newer one runs (at most one slice left unharvested, so
+        # the two pinned status buffers never overlap); with no newer slice, harvest the last one
+        while len(self.pending_slices) > 1 or (self.pending_slices and (
+                not self._occupied() or self.status_event[self.pending_slices[0][0]].query())):
+            done += self._harvest(*self.pending_slices.popleft())
+        self._complete()
         self.busy_time += time.perf_counter() - t0
-        self.slices += 1
         return done
 
+    def _occupied(self) -> bool:
+        return any(x is not None for x in self.slots)
+
     def run_until_idle(self):
-        while self.pending():
+        while self.pending() or self.pending_slices:
             self.step()
+        self._complete(wait=True)
         return self.completed
 
     def stats(self) -> dict:

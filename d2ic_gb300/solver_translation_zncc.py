@@ -31,7 +31,10 @@ def match_centers_device(centers, ref_image, def_image, win: int, search: int, d
     device = torch.device(device if device is not None else "cuda")
     ref = as_device_image(ref_image, device)
     dfm = as_device_image(def_image, device)
-    c = torch.as_tensor(np.asarray(centers, dtype=np.float32).reshape(-1, 2), device=device).contiguous()
+    if isinstance(centers, torch.Tensor):
+        c = centers.to(device=device, dtype=torch.float32).reshape(-1, 2).contiguous()
+    else:
+        c = torch.as_tensor(np.asarray(centers, dtype=np.float32).reshape(-1, 2), device=device).contiguous()
     n = c.shape[0]
     u = torch.empty((n, 2), dtype=torch.float32, device=device)
     s = torch.empty((n,), dtype=torch.float32, device=device)
