@@ -224,9 +224,47 @@ def shape_functions(xi, eta) -> np.ndarray:
                      0.25 * (1 + xi) * (1 + eta), 0.25 * (1 - xi) * (1 + eta)], axis=-1)
 
 
+def local_coordinates_device(pixel_coords, pixel_nodes, nodes_coord, iters: int = 10, device=None):
+    """:func:`local_coordinates` on the GPU (``d2ic_local_coordinates``): the same FP64 operation
+    sequence with correctly rounded operations, so the results are bit-identical."""
+    import torch
+
+    from . import _lib
+    from ._lib import ptr
+    dev = torch.device(device if device is not None else "cuda")
+    pc = torch.from_numpy(np.ascontiguousarray(pixel_coords, dtype=np.float64)).to(dev)
+    pn = torch.from_numpy(np.ascontiguousarray(pixel_nodes, dtype=np.int32)).to(dev)
+    X = torch.from_numpy(np.ascontiguousarray(nodes_coord, dtype=np.float64)).to(dev)
+    n = int(pc.shape[0])
+    xi = torch.empty(max(n, 1), dtype=torch.float64, device=dev)
+    eta = torch.empty_like(xi)
+    _lib.call("d2ic_local_coordinates", ptr(pc), ptr(pn), ptr(X), n, int(iters), ptr(xi), ptr(eta),
+              _lib.stream_handle())
+    return xi[:n].cpu().numpy(), eta[:n].cpu().numpy()
+
+
+def _gpu_available() -> bool:
+    try:
+        import torch
+
+        from . import _lib
+        if not torch.cuda.is_available():
+            return False
+        _lib.load()
+        return True
+    except Exception:
+        return False
+
+
 def compute_pixel_shape_functions(pixel_coords, pixel_nodes, nodes_coord):
-    """``(pixel_N (Np,4), xi_eta (Np,2))`` (d2ic/pixel_assets.py:240-274)."""
-    xi, eta = local_coordinates(pixel_coords, pixel_nodes, nodes_coord)
+    """``(pixel_N (Np,4), xi_eta (Np,2))`` (d2ic/pixel_assets.py:240-274).
+
+    The Newton inverse map runs on the GPU when one is present (bit-identical to
+    the host form, which runs otherwise)."""
+    if _gpu_available() and np.asarray(pixel_coords).shape[0] > 0:
+        xi, eta = local_coordinates_device(pixel_coords, pixel_nodes, nodes_coord)
+    else:
+        xi, eta = local_coordinates(pixel_coords, pixel_nodes, nodes_coord)
     return shape_functions(xi, eta), np.stack([xi, eta], axis=1)
 
 

@@ -148,6 +148,16 @@ D2IC_API int d2ic_pack_pixels(const int *colrow, const float *xieta, int n,
                      const float *coeff1, int H, int W, int pad, int cpitch, int kind,
                      d2ic_pixrec_t *out, void *stream);
 
+/* ---- pixel-asset setup (replaces the Newton inverse map of build_pixel_assets,
+ *      d2ic/pixel_assets.py:240-294) ---- */
+
+/* (xi, eta) of each pixel in its Q4 element by at most `iters` Newton steps from
+ * (0, 0), FP64 with correctly rounded operations in the host restatement's order
+ * (bit-identical results).  pixel_coords: 2 * n_pix; pixel_nodes: 4 * n_pix
+ * node indices; nodes: 2 * n_nodes; xi, eta: n_pix each.  Device pointers. */
+D2IC_API int d2ic_local_coordinates(const double *pixel_coords, const int *pixel_nodes, const double *nodes,
+                                    long long n_pix, int iters, double *xi, double *eta, void *stream);
+
 /* ---- local Gauss-Newton refinement (replaces LocalGaussNewtonSolver,
  *      d2ic/solver_local_gn.py:34-414) ---- */
 

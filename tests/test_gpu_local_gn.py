@@ -58,3 +58,20 @@ def test_cg_then_local_chain(cuda):
     u = np.asarray(out.results[0].u_nodal)
     assert np.isfinite(u).all()
     assert 0 < np.abs(u - np.asarray(u_cg)).max() < 0.2                 # a few relaxed local steps from CG
+
+
+def test_device_local_coordinates_bit_exact(cuda):
+    """GPU Newton inverse map == host restatement, bit for bit, on distorted quads."""
+    from d2ic_gb300.pixel_assets import local_coordinates, local_coordinates_device
+    rng = np.random.default_rng(21)
+    n_el = 400
+    base = np.array([[0.0, 0.0], [10.0, 0.0], [10.0, 10.0], [0.0, 10.0]])
+    nodes = (base[None] + rng.normal(0, 1.2, (n_el, 4, 2)) + 20 * rng.integers(0, 30, (n_el, 1, 2))).reshape(-1, 2)
+    pn = np.arange(4 * n_el).reshape(n_el, 4).repeat(50, axis=0)
+    w = rng.uniform(0.05, 0.95, (n_el * 50, 2))
+    q = nodes[pn]
+    pc = ((1 - w[:, :1]) * (1 - w[:, 1:]) * q[:, 0] + w[:, :1] * (1 - w[:, 1:]) * q[:, 1]
+          + w[:, :1] * w[:, 1:] * q[:, 2] + (1 - w[:, :1]) * w[:, 1:] * q[:, 3])
+    xh, eh = local_coordinates(pc, pn, nodes)
+    xd, ed = local_coordinates_device(pc, pn, nodes, device=cuda)
+    assert np.array_equal(xh.view(np.int64), xd.view(np.int64)) and np.array_equal(eh.view(np.int64), ed.view(np.int64))
