@@ -447,20 +447,49 @@ __device__ __forceinline__ void chunk_compute(const d2ic_frame_t &F, const Chunk
         for (int p = lane; p < n; p += 32) one(__ldg(gpix + p));
     }
     const DF js = df_warp_sum(DF{jr, 0.f});
+    // The 8 nodal partials summed over the warp by a reduce-scatter butterfly: at each of the
+    // steps over lane bits 4, 3, 2 a lane keeps half of its values and adds its partner's copy of
+    // that half (7 shuffles instead of 40); bits 1, 0 finish the sums.  Value k = (gx_0..3,
+    // gy_0..3)[k] ends in lane 16 (k >> 2) + 8 ((k >> 1) & 1) + 4 (k & 1).
+    float v4[4];
+    {
+        const bool b = (lane >> 4) & 1;
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        gxa[a] = warp_sum_f(gxa[a]);
-        gya[a] = warp_sum_f(gya[a]);
+        for (int q = 0; q < 4; ++q) {
+            const float give = b ? gxa[q] : gya[q];
+            const float keep = b ? gya[q] : gxa[q];
+            v4[q] = keep + __shfl_xor_sync(0xffffffffu, give, 16);
+        }
     }
+    float v2[2];
+    {
+        const bool b = (lane >> 3) & 1;
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const float give = b ? v4[q] : v4[q + 2];
+            const float keep = b ? v4[q + 2] : v4[q];
+            v2[q] = keep + __shfl_xor_sync(0xffffffffu, give, 8);
+        }
+    }
+    float v1;
+    {
+        const bool b = (lane >> 2) & 1;
+        const float give = b ? v2[0] : v2[1];
+        const float keep = b ? v2[1] : v2[0];
+        v1 = keep + __shfl_xor_sync(0xffffffffu, give, 4);
+    }
+    v1 += __shfl_xor_sync(0xffffffffu, v1, 2);
+    v1 += __shfl_xor_sync(0xffffffffu, v1, 1);
+    // lane a < 4 takes gx_a (k = a) and gy_a (k = 4 + a)
+    const int la = lane & 3;
+    const float gxs = __shfl_sync(0xffffffffu, v1, 8 * ((la >> 1) & 1) + 4 * (la & 1));
+    const float gys = __shfl_sync(0xffffffffu, v1, 16 + 8 * ((la >> 1) & 1) + 4 * (la & 1));
     if (lane == 0 && tw > 0) F.chunk_tile[m.c] = tile_origin(m.box0, ux, uy);
     // lane a stores node a's partial in the chunk's slot of that node; node 0's slot also
     // carries the chunk's sum of r^2 (double-float), so every chunk is counted exactly once
-    if (lane < 4) {
-        const float gx = lane == 0 ? gxa[0] : lane == 1 ? gxa[1] : lane == 2 ? gxa[2] : gxa[3];
-        const float gy = lane == 0 ? gya[0] : lane == 1 ? gya[1] : lane == 2 ? gya[2] : gya[3];
+    if (lane < 4)
         reinterpret_cast<float4 *>(F.node_grad)[(size_t)m.slot * F.n_nodes + m.nd] =
-            make_float4(gx, gy, lane == 0 ? js.hi : 0.f, lane == 0 ? js.lo : 0.f);
-    }
+            make_float4(gxs, gys, lane == 0 ? js.hi : 0.f, lane == 0 ? js.lo : 0.f);
     __syncwarp();                                   // every lane is done with the staged buffers
 }
 
