@@ -71,8 +71,10 @@ class ImplicitAdjoint:
         inv[active, 0, 0] = D[active, 2] / det[active]
         inv[active, 1, 1] = D[active, 0] / det[active]
         inv[active, 0, 1] = inv[active, 1, 0] = -D[active, 1] / det[active]
-        self.Minv = torch.as_tensor(inv, dtype=torch.float64, device=self.dev)
+        self.Minv = torch.as_tensor(inv, dtype=torch.float64, device=self.dev).contiguous()
         self.active = torch.as_tensor(active, device=self.dev)
+        self._active_u8 = self.active.to(torch.uint8).contiguous()
+        self._pcg_work = None
 
     def matvec(self, V: torch.Tensor) -> torch.Tensor:
         """H V for V of shape (Nn, 2, K) (float64 in, float64 out; the kernels run in FP32)."""
@@ -90,31 +92,22 @@ class ImplicitAdjoint:
         return Y.to(torch.float64)
 
     def solve(self, B: torch.Tensor, rtol: float = 1e-7, max_iter: int = 2000):
-        """X = H^-1 B column by column (block-Jacobi PCG, all columns in lock step)."""
-        B = B.to(torch.float64)
-        mask = self.active[:, None, None].to(B.dtype)
-        B = B * mask
-        X = torch.zeros_like(B)
-        R = B.clone()
-        Z = torch.einsum("nij,njk->nik", self.Minv, R)
-        P = Z.clone()
-        rz = (R * Z).sum(dim=(0, 1))
-        bn = torch.sqrt((B * B).sum(dim=(0, 1))).clamp_min(1e-300)
-        it = 0
-        for it in range(1, max_iter + 1):
-            AP = self.matvec(P) * mask
-            pap = (P * AP).sum(dim=(0, 1))
-            a = torch.where(pap > 0, rz / pap, torch.zeros_like(rz))
-            X += P * a
-            R -= AP * a
-            rn = torch.sqrt((R * R).sum(dim=(0, 1)))
-            if bool((rn <= rtol * bn).all()):
-                break
-            Z = torch.einsum("nij,njk->nik", self.Minv, R)
-            rz_new = (R * Z).sum(dim=(0, 1))
-            P = Z + P * torch.where(rz > 0, rz_new / rz, torch.zeros_like(rz))
-            rz = rz_new
-        self.last_iters = it
+        """X = H^-1 B column by column: block-Jacobi PCG, all columns in lock step, run by
+        ``d2ic_pcg_solve`` (FP64 vectors, FP32 Hessian matvec, deterministic reductions)."""
+        import ctypes
+        L = self.L
+        B = B.to(device=self.dev, dtype=torch.float64).contiguous()
+        K = int(B.shape[2])
+        nb = _lib.load().d2ic_pcg_work_bytes(L.n_nodes, K, L.node_chunk_k)
+        if self._pcg_work is None or self._pcg_work.numel() < nb:
+            self._pcg_work = torch.empty(nb, dtype=torch.uint8, device=self.dev)
+        X = torch.empty_like(B)
+        it = ctypes.c_int(0)
+        _lib.call("d2ic_pcg_solve", ptr(self.desc), L.n_chunks, L.n_nodes, L.node_chunk_k, ptr(self.hess),
+                  self.inv_np, self.alpha, ptr(self.Minv), ptr(self._active_u8), ptr(B), ptr(X), K, float(rtol),
+                  int(max_iter), ptr(self._pcg_work), self._pcg_work.numel(), ctypes.addressof(it),
+                  _lib.stream_handle())
+        self.last_iters = int(it.value)
         return X
 
     # -- the mixed term and its adjoint ---------------------------------------------------------------
@@ -193,7 +186,9 @@ def strain_jvp(u, du, nodes, nbr_index, nbr_degree, gauge_length: float = 0.0, e
         r = torch.linalg.norm(dX, dim=2)
         w = w * torch.exp(-(r / (gauge_length + 1e-12)) ** 2)
     A = torch.einsum("nk,nki,nkj->nij", w, dX, dX) + eps * torch.eye(2, dtype=torch.float64, device=dev)
-    Ainv = torch.linalg.inv(A)
+    det = A[:, 0, 0] * A[:, 1, 1] - A[:, 0, 1] * A[:, 1, 0]          # closed-form 2x2 inverse
+    Ainv = torch.stack([torch.stack([A[:, 1, 1], -A[:, 0, 1]], -1),
+                        torch.stack([-A[:, 1, 0], A[:, 0, 0]], -1)], -2) / det[:, None, None]
 
     def grad_of(v):                         # v (..., Nn, 2) -> G (..., Nn, 2, 2), G[c][i] = d v_c / d x_i
         dv = v[..., nid, :] - v[..., :, None, :]

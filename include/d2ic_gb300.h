@@ -148,6 +148,20 @@ D2IC_API int d2ic_pack_pixels(const int *colrow, const float *xieta, int n,
                      const float *coeff1, int H, int W, int pad, int cpitch, int kind,
                      d2ic_pixrec_t *out, void *stream);
 
+/* ---- adjoint linear solves: block-Jacobi PCG on the exact Hessian, K right-hand sides ---- */
+
+/* Bytes of device scratch d2ic_pcg_solve needs (256-byte aligned base). */
+D2IC_API size_t d2ic_pcg_work_bytes(int n_nodes, int K, int node_chunk_k);
+
+/* X = H^-1 B for B, X (n_nodes, 2, K) FP64 (column index fastest), H applied by
+ * d2ic_hessian_matvec from chunk_hess, Minv (n_nodes, 2, 2) FP64 inverse diagonal
+ * blocks (zero for inactive dofs), active (n_nodes) 0/1 mask.  Stops when every
+ * column has ||R|| <= rtol ||B|| or after max_iter iterations (*iters_out). */
+D2IC_API int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
+                            const float *chunk_hess, float inv_np, float alpha_reg, const double *Minv,
+                            const unsigned char *active, const double *B, double *X, int K, double rtol,
+                            int max_iter, void *work, size_t work_bytes, int *iters_out, void *stream);
+
 /* ---- pixel-asset setup (replaces the Newton inverse map of build_pixel_assets,
  *      d2ic/pixel_assets.py:240-294) ---- */
 
