@@ -935,7 +935,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         if (na == 0) break;
         const bool trr = tr && round < trace_rounds;
         if (trr) trace[7 * round + 0] = gtimer();
-        // ---- P phase: chunk g of the active list goes to global warp g mod (warps in grid) ----
+        // ---- P phase: chunks of the active list spread over the warps (see below) ----
         {
             const int total = ld_vol(&C.h->total_chunks);
             const bool cached = na <= FCACHE;
@@ -1010,14 +1010,22 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             CandRaw r0{}, r1{};
             Stage st0{}, st1{};
             bool p_ok = true;
-            if (gw < total) {
-                m0 = fetch_meta(gw);
+            // One frame: warp gw takes the contiguous chunk range [cb, ce) (neighbouring elements
+            // share coefficient rows in cache; measured faster).  Several frames: chunk g goes to
+            // warp g mod (warps), so that every step of the pass spans few frames (measured faster
+            // for batches of small frames).
+            const bool contiguous = na == 1;
+            const int cb = contiguous ? (int)(((long long)gw * total) / nw) : gw;
+            const int ce = contiguous ? (int)(((long long)(gw + 1) * total) / nw) : total;
+            const int cs = contiguous ? 1 : nw;
+            if (cb < ce) {
+                m0 = fetch_meta(cb);
                 st0 = issue(m0, pipe_i, r0);
-                if (gw + nw < total) m1 = fetch_meta(gw + nw);
+                if (cb + cs < ce) m1 = fetch_meta(cb + cs);
             }
-            for (int g = gw; g < total; g += nw) {
-                const bool has1 = g + nw < total;
-                if (g + 2 * nw < total) m2 = fetch_meta(g + 2 * nw);
+            for (int g = cb; g < ce; g += cs) {
+                const bool has1 = g + cs < ce;
+                if (g + 2 * cs < ce) m2 = fetch_meta(g + 2 * cs);
                 if (has1) st1 = issue(m1, pipe_i + 1, r1);
                 const bool got = mbar_wait(&s_bar[wid][pipe_i & 1], (pipe_i >> 1) & 1u);
                 if (!__all_sync(0xffffffffu, got)) {
@@ -1051,7 +1059,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             __syncwarp();
             if (p_ok) {
                 cur = 0;
-                for (int g = gw; g < total; g += nw) {
+                for (int g = cb; g < ce; g += cs) {
                     int f, base;
                     if (cached) {
                         while (cur + 1 < na && s_cpre[cur + 1] <= g) ++cur;
