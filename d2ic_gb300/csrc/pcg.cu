@@ -122,13 +122,15 @@ __global__ void __launch_bounds__(PT) pcg_dir(int n_nodes, int K, const double *
     }
 }
 
-// out[k] = sum over blocks of part[b][k], in block order
+// out[k] = sum over blocks of part[b][k]: one warp per column, lane l sums blocks l, l + 32, ...
+// in order, then a fixed shuffle tree (deterministic)
 __global__ void pcg_reduce(int nb, int K, const double *__restrict__ part, double *__restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (k >= K) return;
     double s = 0.0;
-    for (int b = 0; b < nb; ++b) s += part[(size_t)b * K + k];
-    out[k] = s;
+    for (int b = lane; b < nb; b += 32) s += part[(size_t)b * K + k];
+    s = warp_sum_d(s);
+    if (lane == 0) out[k] = s;
 }
 
 struct PcgWork {
@@ -194,10 +196,10 @@ extern "C" int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n
     // slots that no chunk owns must read as 0; owned ones are rewritten by every matvec
     cudaError_t e = cudaMemsetAsync(w.slots, 0, sizeof(float) * (size_t)node_chunk_k * v, s);
     if (e != cudaSuccess) return cuda_status(e, "pcg slots");
-    const int rb = (K + 127) / 128;
+    const int rb = (K + 7) / 8;                    // pcg_reduce: 8 warps (columns) per block
     pcg_init<<<nb, PT, 0, s>>>(n_nodes, K, B, active, Minv, X, w.R, w.Z, w.P, w.Pf, w.part_a, w.part_b);
-    pcg_reduce<<<rb, 128, 0, s>>>(nb, K, w.part_a, w.rz);
-    pcg_reduce<<<rb, 128, 0, s>>>(nb, K, w.part_b, w.bb);
+    pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_a, w.rz);
+    pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_b, w.bb);
     D2IC_CHECK_LAUNCH("pcg init");
     double *host = (double *)malloc(sizeof(double) * 2 * K);
     if (!host) {
@@ -218,10 +220,10 @@ extern "C" int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n
                                  stream);
         if (st) break;
         pcg_pap<<<nb, PT, 0, s>>>(n_nodes, K, w.P, w.AP, active, w.part_a);
-        pcg_reduce<<<rb, 128, 0, s>>>(nb, K, w.part_a, w.pap);
+        pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_a, w.pap);
         pcg_step<<<nb, PT, 0, s>>>(n_nodes, K, rz, w.pap, active, Minv, X, w.R, w.Z, w.P, w.AP, w.part_a, w.part_b);
-        pcg_reduce<<<rb, 128, 0, s>>>(nb, K, w.part_a, w.rr);
-        pcg_reduce<<<rb, 128, 0, s>>>(nb, K, w.part_b, rz_new);
+        pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_a, w.rr);
+        pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_b, rz_new);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(h_rr, w.rr, sizeof(double) * K, cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
