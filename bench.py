@@ -62,8 +62,8 @@ def parse():
     p.add_argument("--serve-slice", type=int, default=16)
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--batch-frames", type=int, default=64)
-    p.add_argument("--batch-sides", default="512,1024,2048",
-                   help="image sides drawn for the uneven batch (the full set adds 3072,4096)")
+    p.add_argument("--batch-sides", default="512,1024,2048,3072,4096",
+                   help="image sides drawn for the uneven batch")
     p.add_argument("--no-local", action="store_true")
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--adjoint-realisations", type=int, default=256)
@@ -303,20 +303,29 @@ def run_serving(args, dev, sides=(512, 1024, 2048), n_seq=None, label="mixed_str
     t_served = time.perf_counter() - t0
     diff = max(float(np.abs(r.u - plain_u[(r.seq_id, r.frame_index)]).max()) for r in reqs)
     served_fps = len(reqs) / t_served
-    # online: Poisson arrivals at half the measured served throughput
-    rate = 0.5 * served_fps
-    rng = np.random.default_rng(4)
-    offsets = np.cumsum(rng.exponential(1.0 / rate, len(order)))
-    reqs_on = served_pass(offsets)
-    lat = np.array([r.latency for r in reqs_on])
+    # online: Poisson arrivals at fractions of the measured served throughput (rate sweep)
+    sweep = []
+    for frac in (0.25, 0.5, 0.75, 1.0):
+        rate_k = frac * served_fps
+        rng = np.random.default_rng(4)
+        offs = np.cumsum(rng.exponential(1.0 / rate_k, len(order)))
+        t_on = time.perf_counter()
+        reqs_k = served_pass(offs)
+        wall = time.perf_counter() - t_on
+        lat_k = np.array([r.latency for r in reqs_k])
+        sweep.append({"offered_frames_per_s": rate_k, "achieved_frames_per_s": len(reqs_k) / wall,
+                      "latency_ms_p50": 1000 * float(np.percentile(lat_k, 50)),
+                      "latency_ms_p99": 1000 * float(np.percentile(lat_k, 99))})
+    rate = sweep[1]["offered_frames_per_s"]
+    lat = None
     return {"workload": label, "sequences": len(seqs), "frames": len(order),
             "image_sides": sorted({int(wl.ref.shape[0]) for wl in seqs}), "roi_pixels_per_pass": int(n_pix),
             "plain_frames_per_s": len(order) / t_plain, "served_frames_per_s": served_fps,
             "speedup": served_fps / (len(order) / t_plain), "max_abs_diff_vs_plain_px": diff,
             "plain_latency_ms_p50": 1000 * float(np.percentile(plain_lat, 50)),
             "plain_latency_ms_p99": 1000 * float(np.percentile(plain_lat, 99)),
-            "online_rate_frames_per_s": rate, "latency_ms_p50": 1000 * float(np.percentile(lat, 50)),
-            "latency_ms_p99": 1000 * float(np.percentile(lat, 99)), "slots": args.serve_slots,
+            "online_rate_frames_per_s": rate, "latency_ms_p50": sweep[1]["latency_ms_p50"],
+            "latency_ms_p99": sweep[1]["latency_ms_p99"], "rate_sweep": sweep, "slots": args.serve_slots,
             "slice_rounds": args.serve_slice, "graphs": srv.graph is not None}
 
 

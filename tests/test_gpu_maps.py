@@ -45,3 +45,29 @@ def test_discrepancy_map_matches_oracle(cuda):
     assert ok.sum() > 0.8 * 144 * 144
     assert np.abs(gmap[ok] - omap[ok]).max() <= 2e-3                  # grey levels (FP32 weights vs FP64)
     assert abs(res.diagnostics.info["discrepancy_rms"] - orms) <= 1e-4 * max(orms, 1.0)
+
+
+@pytest.mark.gpu
+def test_batch_writes_per_frame_fields(cuda, tmp_path):
+    """BatchMeshBased(save_per_frame=True) writes frame_XXXX.npz with u_nodal, strain and the
+    discrepancy map (d2ic/batch_mesh_based.py:174-185)."""
+    from dataclasses import replace
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300.synthetic import Translation, rect_mask, speckle_sequence
+    H = W = 128
+    ref, frames = speckle_sequence(H, W, [Translation(0.3, 0.1), Translation(0.5, 0.2)], seed=9,
+                                   noise_seeds=[9, 10, 11])
+    mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, W, 96, 96), 16)
+    assets = replace(assets, pixel_data=d2.build_pixel_assets(mesh, ref, 1.0, assets.roi_mask))
+    cfg = d2.MeshDICConfig(max_iters=100, tol=1e-3, reg_strength=0.1, compute_discrepancy_map=True)
+    dic = d2.DICMeshBased(mesh, d2.GlobalCGSolver(device=cuda), cfg)
+    batch = d2.BatchMeshBased(ref, assets, dic, d2.BatchConfig(warm_start_from_previous=True, save_per_frame=True,
+                                                               per_frame_dir=str(tmp_path)))
+    batch.before(frames)
+    out = batch.sequence(frames)
+    for k in range(2):
+        z = np.load(tmp_path / f"frame_{k:04d}.npz")
+        assert np.array_equal(z["u_nodal"], np.asarray(out.results[k].u_nodal))
+        assert z["strain"].shape == (mesh.nodes_xy.shape[0], 3)
+        assert z["discrepancy_ref"].shape == (H, W) and np.isfinite(z["discrepancy_ref"]).sum() > 0.5 * 96 * 96
