@@ -27,6 +27,7 @@ from .propagators import DisplacementPropagatorBase, PreviousDisplacementPropaga
 from .solver_translation_zncc import TranslationZNCCSolver
 from .solver_global_cg import GlobalCGSolver
 from .solver_local_gn import LocalGaussNewtonSolver, LocalGNResult
+from .outputs import save_fields_sequence, save_frame_npz
 
 __all__ = [
     "Array", "InitMotionConfig", "MeshDICConfig", "DICResult", "DICDiagnostics", "BatchConfig", "BatchResult",
@@ -36,4 +37,5 @@ __all__ = [
     "small_strain_nodes_lsq", "SolverBase", "DICBase", "DICInitMotion", "DICMeshBased", "BatchBase",
     "BatchMeshBased", "DisplacementPropagatorBase", "PreviousDisplacementPropagator", "ConstantVelocityPropagator",
     "TranslationZNCCSolver", "GlobalCGSolver", "LocalGaussNewtonSolver", "LocalGNResult",
+    "save_fields_sequence", "save_frame_npz",
 ]

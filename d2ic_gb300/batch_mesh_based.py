@@ -2,7 +2,8 @@
 
 ``run(images) = end(sequence(images))`` after ``before(images)``; per frame:
 warm start (propagator, else the previous solution), optional chained local
-refinement pipeline, optional per-frame ``.npz`` (``u_nodal``, ``strain``).
+refinement pipeline, optional per-frame ``.npz`` (``u_nodal``, ``strain``,
+``discrepancy_ref``; writers in ``outputs.py``).
 PNG export needs matplotlib, which this package does not use.
 """
 from __future__ import annotations
@@ -17,8 +18,49 @@ import numpy as np
 from .dataclasses import BatchConfig, BatchDiagnostics, BatchResult, DICResult
 from .dic_mesh_based import DICMeshBased
 from .mesh_assets import MeshAssets
+from .outputs import save_frame_npz
 from .propagators import DisplacementPropagatorBase
 from .types import Array
+
+
+def _prefetched(images):
+    """The frames as device tensors, each host->device copy queued on a copy stream one frame
+    ahead, so that frame k+1 travels while frame k is solved (pinned host frames copy
+    asynchronously; device frames pass through)."""
+    import torch
+    if not torch.cuda.is_available():
+        yield from images
+        return
+    dev = torch.device("cuda", torch.cuda.current_device())
+    copy = torch.cuda.Stream(device=dev)
+
+    def start(img):
+        if isinstance(img, torch.Tensor) and img.is_cuda:
+            return img, None
+        src = img if isinstance(img, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(img, dtype=np.float32))
+        with torch.cuda.stream(copy):
+            d = src.to(dev, dtype=torch.float32, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(copy)
+        return d, ev
+
+    def finish(pair):
+        d, ev = pair
+        if ev is not None:
+            cur = torch.cuda.current_stream(dev)
+            cur.wait_event(ev)
+            d.record_stream(cur)
+        return d
+
+    it = iter(images)
+    try:
+        nxt = start(next(it))
+    except StopIteration:
+        return
+    for img in it:
+        cur_pair, nxt = nxt, start(img)
+        yield finish(cur_pair)
+    yield finish(nxt)
 
 
 class BatchBase(ABC):
@@ -86,7 +128,7 @@ class BatchMeshBased(BatchBase):
         per_frame: list[DICResult] = []
         u_prev = None
         u_prevprev = None
-        for k, Idef in enumerate(images):
+        for k, Idef in enumerate(_prefetched(images)):
             t0 = time.perf_counter()
             if progress or verbose:
                 print(f"[Batch] Frame {k + 1}{'' if n_frames is None else '/' + str(n_frames)}: start")
@@ -104,11 +146,7 @@ class BatchMeshBased(BatchBase):
             if latencies is not None:
                 latencies.append(time.perf_counter() - t0)
             if save:
-                payload = {"u_nodal": np.asarray(res.u_nodal), "strain": np.asarray(res.strain)}
-                disc = (res.pixel_maps or {}).get("discrepancy_ref")
-                if disc is not None:
-                    payload["discrepancy_ref"] = np.asarray(disc)
-                np.savez_compressed(out_dir / f"frame_{k:04d}.npz", **payload)
+                save_frame_npz(out_dir / f"frame_{k:04d}.npz", res)
             u_prevprev = u_prev
             u_prev = res.u_nodal
             if progress or verbose:

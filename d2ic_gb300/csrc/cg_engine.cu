@@ -270,6 +270,17 @@ __device__ __forceinline__ int find_slot(const int *pre, int n, int x) {
     return lo;
 }
 
+// the same search over a copy of the prefix sums in shared memory
+__device__ __forceinline__ int find_slot_smem(const int *pre, int n, int x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ---------------------------------------------------------------------------
 // P phase: one chunk per warp, software-pipelined
 // ---------------------------------------------------------------------------
@@ -342,7 +353,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity
 // (lane) a's index and slot rank in lanes 0..3.
 struct ChunkMeta {
     int s, f, c, pb, pe, nd, slot;   // active slot, frame, chunk within the frame, ...
-    int box0, tile;                  // packed pixel-box corner and tile origin (col | row << 16)
+    int box0, box1, tile;            // packed pixel-box corners and tile origin (col | row << 16)
 };
 
 __device__ __forceinline__ ChunkMeta load_meta(const d2ic_frame_t *frames, int f, int c, int lane) {
@@ -354,6 +365,7 @@ __device__ __forceinline__ ChunkMeta load_meta(const d2ic_frame_t *frames, int f
     m.pb = __ldg(F.chunk_begin + c);
     m.pe = __ldg(F.chunk_begin + c + 1);
     m.box0 = __ldg(F.chunk_box + 2 * c);
+    m.box1 = __ldg(F.chunk_box + 2 * c + 1);
     m.tile = F.tile_w > 0 ? __ldcg(F.chunk_tile + c) : TILE_NONE;   // rewritten every pass: L2
     m.nd = 0;
     m.slot = 0;
@@ -407,8 +419,55 @@ __device__ __forceinline__ void chunk_compute(const d2ic_frame_t &F, const Chunk
         uy[a] = __shfl_sync(0xffffffffu, uc.y, a);
     }
     const Img im{F.coeff, F.W, F.H, F.cpitch, F.pad};
+    // Whole chunk inside the tile: a pixel's displacement is a convex combination of its
+    // element's nodal candidates, so its stencil corner lies in the chunk's pixel box shifted by
+    // [floor(min u), floor(max u)] (taken with 0.5 px of slack).  Then no pixel needs the
+    // per-pixel test or the global-memory path.
+    bool fast = false;
+    if (tiled && staged && n <= D2IC_CHUNK_MAX) {
+        bool fin = true;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) fin = fin && isfinite(ux[a]) && isfinite(uy[a]);
+        if (fin) {
+            const float mnx = fminf(fminf(ux[0], ux[1]), fminf(ux[2], ux[3]));
+            const float mxx = fmaxf(fmaxf(ux[0], ux[1]), fmaxf(ux[2], ux[3]));
+            const float mny = fminf(fminf(uy[0], uy[1]), fminf(uy[2], uy[3]));
+            const float mxy = fmaxf(fmaxf(uy[0], uy[1]), fmaxf(uy[2], uy[3]));
+            const int lx0 = (m.box0 & 0xffff) + (int)safe_floor(mnx - 0.5f) - 1 - tx0;
+            const int lx1 = (m.box1 & 0xffff) + (int)safe_floor(mxx + 0.5f) - 1 - tx0;
+            const int ly0 = (int)((unsigned)m.box0 >> 16) + (int)safe_floor(mny - 0.5f) - 1 - ty0;
+            const int ly1 = (int)((unsigned)m.box1 >> 16) + (int)safe_floor(mxy + 0.5f) - 1 - ty0;
+            fast = lx0 >= 0 && lx1 <= tw - 4 && ly0 >= 0 && ly1 <= th - 4;
+        }
+    }
     float jr = 0.f;
     float gxa[4] = {0.f, 0.f, 0.f, 0.f}, gya[4] = {0.f, 0.f, 0.f, 0.f};
+    // fast path: the stencil corner is clamped into the tile only as a guard of the shared-memory
+    // bounds (it is already inside)
+    auto one_fast = [&](const uint4 r4) {
+        const int x = (int)(r4.x & 0xffffu), y = (int)(r4.x >> 16);
+        const float I1 = __uint_as_float(r4.y), xi = __uint_as_float(r4.z), eta = __uint_as_float(r4.w);
+        const float a0 = 0.5f * (1.f - xi), a1 = 0.5f * (1.f + xi);
+        const float b0 = 0.5f * (1.f - eta), b1 = 0.5f * (1.f + eta);
+        const float N[4] = {a0 * b0, a1 * b0, a1 * b1, a0 * b1};
+        const float dx = N[0] * ux[0] + N[1] * ux[1] + N[2] * ux[2] + N[3] * ux[3];
+        const float dy = N[0] * uy[0] + N[1] * uy[1] + N[2] * uy[2] + N[3] * uy[3];
+        int ix, iy;
+        float tx, ty;
+        split_coord(x, dx, ix, tx);
+        split_coord(y, dy, iy, ty);
+        float gx, gy;
+        const int lx = min(max(ix - 1 - tx0, 0), tw - 4), ly = min(max(iy - 1 - ty0, 0), th - 4);
+        const float v = sample_cubic_tile(tile, tw, lx, ly, tx, ty, gx, gy);
+        const float r = v - I1;
+        jr += r * r;
+        const float rgx = r * gx, rgy = r * gy;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            gxa[a] += rgx * N[a];
+            gya[a] += rgy * N[a];
+        }
+    };
     auto one = [&](const uint4 r4) {
         const int x = (int)(r4.x & 0xffffu), y = (int)(r4.x >> 16);
         const float I1 = __uint_as_float(r4.y), xi = __uint_as_float(r4.z), eta = __uint_as_float(r4.w);
@@ -436,7 +495,13 @@ __device__ __forceinline__ void chunk_compute(const d2ic_frame_t &F, const Chunk
             gya[a] += rgy * N[a];
         }
     };
-    if (staged) {
+    if (fast) {
+#pragma unroll 4
+        for (int i = 0; i < D2IC_CHUNK_MAX / 32; ++i) {
+            const int p = lane + 32 * i;
+            if (p < n) one_fast(srec[p]);
+        }
+    } else if (staged) {
 #pragma unroll 4
         for (int i = 0; i < D2IC_CHUNK_MAX / 32; ++i) {
             const int p = lane + 32 * i;
@@ -493,15 +558,16 @@ __device__ __forceinline__ void chunk_compute(const d2ic_frame_t &F, const Chunk
     __syncwarp();                                   // every lane is done with the staged buffers
 }
 
-// One count per distinct node group among a chunk's four nodes (lanes 0..3 hold the node
-// indices); the group's reducer waits until it has as many counts as chunks touch the group.
-__device__ __forceinline__ void count_chunk_groups(int *group_cnt, int nd, int lane) {
-    const int grp = nd / GN;
-    const int g0 = __shfl_sync(0xffffffffu, grp, 0), g1 = __shfl_sync(0xffffffffu, grp, 1),
-              g2 = __shfl_sync(0xffffffffu, grp, 2);
-    const bool first = lane == 0 || (lane == 1 && grp != g0) || (lane == 2 && grp != g0 && grp != g1) ||
-                       (lane == 3 && grp != g0 && grp != g1 && grp != g2);
-    if (lane < 4 && first) atomicAdd(group_cnt + grp, 1);
+// One count per distinct node group among a chunk's four nodes; the group's reducer waits
+// until it has as many counts as chunks touch the group.  Each quad of lanes (4 j .. 4 j + 3)
+// holds the node groups of one chunk (grp < 0: no chunk).
+__device__ __forceinline__ void count_chunk_groups_quad(int *group_cnt, int grp, int lane) {
+    const int q0 = lane & ~3, a = lane & 3;
+    const int g0 = __shfl_sync(0xffffffffu, grp, q0), g1 = __shfl_sync(0xffffffffu, grp, q0 + 1),
+              g2 = __shfl_sync(0xffffffffu, grp, q0 + 2);
+    const bool first = a == 0 || (a == 1 && grp != g0) || (a == 2 && grp != g0 && grp != g1) ||
+                       (a == 3 && grp != g0 && grp != g1 && grp != g2);
+    if (grp >= 0 && first) atomicAdd(group_cnt + grp, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -600,7 +666,23 @@ __device__ __forceinline__ void node_post(const d2ic_frame_t &F, const FInfo &fi
 // ---------------------------------------------------------------------------
 // R step (last block at the end-of-round barrier)
 // ---------------------------------------------------------------------------
-__device__ void hist_row(const d2ic_frame_t &F, int k, double a, double b, double c) {
+// The descriptor scalars the control step reads, loaded once at its start.
+struct FConst {
+    float *hist;
+    double tol;
+    float alpha_reg;
+    int max_iter, n_pix;
+};
+
+// Values of a control step that need FP64 division or square root, computed for the whole
+// warp at once (GB300's FP64 pipe is narrow, so each FP64 instruction is costly): the
+// objective J of this round's point, and, for the state after accepting this point, sqrt(g.g)
+// and the PR+ ratio g.(g - g_prev) / (g_prev.g_prev + 1e-16).
+struct StepVals {
+    double J, gnorm, ratio;
+};
+
+__device__ void hist_row(const FConst &F, int k, double a, double b, double c) {
     if (F.hist && k < F.max_iter) {
         F.hist[3 * k + 0] = (float)a;
         F.hist[3 * k + 1] = (float)b;
@@ -621,8 +703,10 @@ __device__ void accept_point(FrameState &S, double J, double gg, double gdiff) {
     S.idp = 1 - S.idp;
 }
 
-__device__ void start_iter(FrameState &S, const d2ic_frame_t &F) {
-    S.gnorm = sqrt(S.gg_cur);
+// Called right after accept_point of this round's point, so v.gnorm = sqrt(S.gg_cur) and
+// v.ratio = S.gdiff_cur / (S.gg_prev + 1e-16).
+__device__ void start_iter(FrameState &S, const FConst &F, const StepVals &v) {
+    S.gnorm = v.gnorm;
     if (S.gnorm < F.tol) {                       // stop branch: k unchanged
         hist_row(F, S.k, S.J_cur, S.gnorm, 0.0);
         S.state = ST_DONE;
@@ -630,7 +714,7 @@ __device__ void start_iter(FrameState &S, const d2ic_frame_t &F) {
     }
     double beta = 0.0;
     if (S.k > 0) {
-        const double x = S.gdiff_cur / (S.gg_prev + 1e-16);
+        const double x = v.ratio;
         beta = (x != x) ? x : fmax(x, 0.0);      // jnp.maximum keeps NaN
     }
     S.beta = (float)beta;
@@ -641,8 +725,8 @@ __device__ void start_iter(FrameState &S, const d2ic_frame_t &F) {
     S.state = ST_TRIAL;
 }
 
-__device__ void frame_decide(FrameState &S, const d2ic_frame_t &F, const double *q, int eval_only) {
-    const double J = 0.5 * q[P_JSUM] / (double)max(F.n_pix, 1) + (double)F.alpha_reg * q[P_EREG];
+__device__ void frame_decide(FrameState &S, const FConst &F, const double *q, const StepVals &v, int eval_only) {
+    const double J = v.J;
     if (J != J || q[P_GG] != q[P_GG]) S.nan_seen = 1;
     S.n_evals += 1;
     // control-flow guard: an iteration takes at most 11 evaluations plus one restart
@@ -657,7 +741,7 @@ __device__ void frame_decide(FrameState &S, const d2ic_frame_t &F, const double 
                 S.state = ST_DONE;
                 return;
             }
-            start_iter(S, F);
+            start_iter(S, F, v);
             return;
         case ST_TRIAL: {
             if (!S.gd_known) {
@@ -675,7 +759,7 @@ __device__ void frame_decide(FrameState &S, const d2ic_frame_t &F, const double 
                 S.k += 1;
                 accept_point(S, J, q[P_GG], q[P_GDIFF]);
                 if (S.k >= F.max_iter) S.state = ST_DONE;
-                else start_iter(S, F);
+                else start_iter(S, F, v);
             } else {
                 S.J_last = J;
                 S.t += 1;
@@ -689,7 +773,7 @@ __device__ void frame_decide(FrameState &S, const d2ic_frame_t &F, const double 
             S.k += 1;
             accept_point(S, J, q[P_GG], q[P_GDIFF]);
             if (S.k >= F.max_iter) S.state = ST_DONE;
-            else start_iter(S, F);
+            else start_iter(S, F, v);
             return;
         default:
             return;
@@ -837,6 +921,12 @@ __device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int
     DF q[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     FrameState S;
     if (lane == 0) S = load_fs(C.fs + f);              // in flight with the partials below
+    FConst fc;
+    fc.hist = F.hist;
+    fc.tol = F.tol;
+    fc.alpha_reg = F.alpha_reg;
+    fc.max_iter = F.max_iter;
+    fc.n_pix = F.n_pix;
     const int nsg = (F.n_groups + GN - 1) / GN;
     const float2 *sp = reinterpret_cast<const float2 *>(F.group_part) + (size_t)F.n_groups * D2IC_NPART;
     for (int g = lane; g < nsg; g += 32) {
@@ -848,11 +938,26 @@ __device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int
     }
 #pragma unroll
     for (int i = 0; i < 5; ++i) q[i] = df_warp_sum(q[i]);
-    if (lane == 0) {
-        double qd[5];
+    // lane i < 5 converts sum i to FP64: one conversion for all five
+    DF sel = q[0];
 #pragma unroll
-        for (int i = 0; i < 5; ++i) qd[i] = df_to_double(q[i]);
-        frame_decide(S, F, qd, eval_only);
+    for (int i = 1; i < 5; ++i)
+        if (lane == i) sel = q[i];
+    const double mine = df_to_double(sel);
+    double qd[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) qd[i] = __shfl_sync(0xffffffffu, mine, i);
+    // one division for two quotients: lane 0 the image term of J, lane 1 the PR+ ratio
+    const double gg_old = __shfl_sync(0xffffffffu, lane == 0 ? S.gg_cur : 0.0, 0);
+    const double num = lane == 0 ? 0.5 * qd[P_JSUM] : qd[P_GDIFF];
+    const double den = lane == 0 ? (double)max(fc.n_pix, 1) : gg_old + 1e-16;
+    const double quo = num / den;
+    StepVals v;
+    v.ratio = __shfl_sync(0xffffffffu, quo, 1);
+    v.gnorm = sqrt(qd[P_GG]);
+    if (lane == 0) {
+        v.J = quo + (double)fc.alpha_reg * qd[P_EREG];
+        frame_decide(S, fc, qd, v, eval_only);
         C.fs[f] = S;
         if (S.state == ST_DONE) atomicExch(&C.h->finished, 1);
     }
@@ -893,6 +998,13 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     // stamps [3] and [4] around it
     const bool tr = trace != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
     int round = 0;
+    // A warp's first chunk of the next round, staged before the round's release (its records,
+    // coefficient tile and the metadata of the chunk after it do not depend on the control step);
+    // used if the active list is unchanged, else drained.
+    bool pf = false;
+    int pf_na = 0, pf_total = 0;
+    ChunkMeta pf_m0{}, pf_m1{};
+    Stage pf_st0{};
 
     // ---- init of newly admitted frames: u <- u0, zero g/d buffers and gradient slots, NaN history ----
     for (int f = 0; f < n_frames; ++f) {
@@ -932,12 +1044,28 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
 
     while (round < max_rounds) {                    // a slice: at most max_rounds rounds, state kept in HBM
         const int na = ld_vol(&C.h->n_active);
+        const int total = ld_vol(&C.h->total_chunks);
+        const int tg = ld_vol(&C.h->total_groups);
         if (na == 0) break;
         const bool trr = tr && round < trace_rounds;
         if (trr) trace[7 * round + 0] = gtimer();
+        // the active list only shrinks within a launch: the same count means the same list
+        const bool pf_use = pf && na == pf_na && total == pf_total;
+        if (pf && !pf_use) {
+            if (!mbar_wait(&s_bar[wid][pipe_i & 1], (pipe_i >> 1) & 1u) && lane == 0) {   // bounded
+                C.h->err = D2IC_WAIT_TIMEOUT;
+                atomicExch(&C.h->abort, 1);
+            }
+            ++pipe_i;
+        }
+        pf = false;
+        const ChunkMeta pm0 = pf_m0, pm1 = pf_m1;
+        const Stage pst0 = pf_st0;
+        pf_m0 = ChunkMeta{};   // constants while the round runs (nothing to keep in registers)
+        pf_m1 = ChunkMeta{};
+        pf_st0 = Stage{};
         // ---- P phase: chunks of the active list spread over the warps (see below) ----
         {
-            const int total = ld_vol(&C.h->total_chunks);
             const bool cached = na <= FCACHE;
             if (cached) {
                 for (int s = threadIdx.x; s <= na; s += NT) {
@@ -972,7 +1100,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             };
             // stage a chunk: TMA bulk copy of its records, 2-D TMA copy of its coefficient tile,
             // loads of its nodal candidate inputs
-            auto issue = [&](const ChunkMeta &m, unsigned i, CandRaw &cr) {
+            auto issue_tma = [&](const ChunkMeta &m, unsigned i) {
                 const d2ic_frame_t &F = frames[m.f];
                 const int n = max(m.pe - m.pb, 0);
                 const unsigned bytes = (unsigned)min(n, D2IC_CHUNK_MAX) * 16u;
@@ -998,12 +1126,20 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                         tensor_load_2d(wbuf + 2 * CHUNK_BYTES + (i & 1) * TILE_BYTES, F.coeff_map, st.tx0 + F.pad,
                                        st.ty0 + F.pad, bar);
                 }
+                return st;
+            };
+            auto load_cand = [&](const ChunkMeta &m, CandRaw &cr) {
                 if (lane < 4) {
+                    const d2ic_frame_t &F = frames[m.f];
                     const FInfo fi = cached ? s_fi[m.s] : frame_info(C.fs + m.f);
                     cr.u = __ldcg(nbuf(F, fi.iu) + m.nd);
                     cr.g = fi.mode != 0 ? __ldcg(nbuf(F, 2 + fi.igc) + m.nd) : make_float2(0.f, 0.f);
                     cr.d = fi.mode == 1 ? __ldcg(nbuf(F, 5 + fi.idp) + m.nd) : make_float2(0.f, 0.f);
                 }
+            };
+            auto issue = [&](const ChunkMeta &m, unsigned i, CandRaw &cr) {
+                const Stage st = issue_tma(m, i);
+                load_cand(m, cr);
                 return st;
             };
             ChunkMeta m0{}, m1{}, m2{};
@@ -1014,14 +1150,34 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             // share coefficient rows in cache; measured faster).  Several frames: chunk g goes to
             // warp g mod (warps), so that every step of the pass spans few frames (measured faster
             // for batches of small frames).
+            // With fewer node groups than warps, group gi is reduced by warp gi (below); when the
+            // spare chunks fit on the other warps, those warps take them, so that the group
+            // reducers finish their own pixel work first and wait for none of it.
             const bool contiguous = na == 1;
-            const int cb = contiguous ? (int)(((long long)gw * total) / nw) : gw;
-            const int ce = contiguous ? (int)(((long long)(gw + 1) * total) / nw) : total;
+            int cb = gw, ce = total;
+            if (contiguous) {
+                const int base = total / nw, extra = total - base * nw;
+                if (tg < nw && extra <= nw - tg) {
+                    const int k = max(gw - tg, 0);
+                    cb = gw * base + min(k, extra);
+                    ce = cb + base + (gw >= tg && k < extra ? 1 : 0);
+                } else {
+                    cb = (int)(((long long)gw * total) / nw);
+                    ce = (int)(((long long)(gw + 1) * total) / nw);
+                }
+            }
             const int cs = contiguous ? 1 : nw;
             if (cb < ce) {
-                m0 = fetch_meta(cb);
-                st0 = issue(m0, pipe_i, r0);
-                if (cb + cs < ce) m1 = fetch_meta(cb + cs);
+                if (pf_use) {
+                    m0 = pm0;
+                    st0 = pst0;
+                    m1 = pm1;
+                    load_cand(m0, r0);
+                } else {
+                    m0 = fetch_meta(cb);
+                    st0 = issue(m0, pipe_i, r0);
+                    if (cb + cs < ce) m1 = fetch_meta(cb + cs);
+                }
             }
             for (int g = cb; g < ce; g += cs) {
                 const bool has1 = g + cs < ce;
@@ -1055,30 +1211,36 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             }
             // ---- count this warp's chunks into their node groups: one fence for the whole pass
             // (a fence per chunk would also wait for the pipeline's prefetch loads in flight) ----
+            // Eight chunks per step: lane 4 j + a reads node a of chunk j, so the node loads of
+            // the eight are in flight together.
             __threadfence();
             __syncwarp();
             if (p_ok) {
-                cur = 0;
-                for (int g = cb; g < ce; g += cs) {
-                    int f, base;
-                    if (cached) {
-                        while (cur + 1 < na && s_cpre[cur + 1] <= g) ++cur;
-                        f = s_act[cur];
-                        base = s_cpre[cur];
-                    } else {
-                        const int s = find_slot(C.cpre, na, g);
-                        f = __ldcg(C.active + s);
-                        base = __ldcg(C.cpre + s);
+                for (int g0 = cb; g0 < ce; g0 += 8 * cs) {
+                    const int g = g0 + (lane >> 2) * cs;
+                    int grp = -1;
+                    int *cnt = nullptr;
+                    if (g < ce) {
+                        int f, base;
+                        if (cached) {
+                            const int sl = na == 1 ? 0 : find_slot_smem(s_cpre, na, g);
+                            f = s_act[sl];
+                            base = s_cpre[sl];
+                        } else {
+                            const int sl = find_slot(C.cpre, na, g);
+                            f = __ldcg(C.active + sl);
+                            base = __ldcg(C.cpre + sl);
+                        }
+                        const d2ic_frame_t &F = frames[f];
+                        grp = __ldg(F.chunk_nodes + 4 * (g - base) + (lane & 3)) / GN;
+                        cnt = F.group_cnt;
                     }
-                    const d2ic_frame_t &F = frames[f];
-                    const int nd = lane < 4 ? __ldg(F.chunk_nodes + 4 * (g - base) + lane) : 0;
-                    count_chunk_groups(F.group_cnt, nd, lane);
+                    count_chunk_groups_quad(cnt, grp, lane);
                 }
             }
             if (trr) trace[7 * round + 1] = gtimer();
             // ---- N work: group gi of the active list goes to global warp gi mod (warps in grid); the
             // warp waits until every chunk with a node in the group has written its slots ----
-            const int tg = ld_vol(&C.h->total_groups);
             int gcur = 0;
             for (int gi = gw; gi < tg; gi += nw) {
                 int s, f, base;
@@ -1179,6 +1341,17 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 }
             }
             if (trr) trace[7 * round + 2] = gtimer();
+            // stage the next round's first chunk (same ranges if the active list is unchanged).  Only
+            // from the shared-memory copy of the list: the global one may be rebuilt meanwhile.
+            if (cached && p_ok && cb < ce && round + 1 < max_rounds && !ld_vol(&C.h->abort)) {
+                cur = 0;
+                pf_m0 = fetch_meta(cb);
+                pf_st0 = issue_tma(pf_m0, pipe_i);
+                if (cb + cs < ce) pf_m1 = fetch_meta(cb + cs);
+                pf = true;
+                pf_na = na;
+                pf_total = total;
+            }
         }
         // ---- end of round: wait until the warp that ran the round's last frame step releases it
         // (rounds_done is monotonic, so a block that arrives after the release passes at once) ----
@@ -1204,6 +1377,8 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         if (trr) trace[7 * round + 5] = gtimer();
         ++round;
     }
+
+    if (pf) mbar_wait(&s_bar[wid][pipe_i & 1], (pipe_i >> 1) & 1u);   // no copy in flight at exit (bounded)
 
 finish:
     // ---- outputs of frames that finished in this launch; running frames report D2IC_RUNNING ----

@@ -71,3 +71,7 @@ def test_batch_writes_per_frame_fields(cuda, tmp_path):
         assert np.array_equal(z["u_nodal"], np.asarray(out.results[k].u_nodal))
         assert z["strain"].shape == (mesh.nodes_xy.shape[0], 3)
         assert z["discrepancy_ref"].shape == (H, W) and np.isfinite(z["discrepancy_ref"]).sum() > 0.5 * 96 * 96
+    seq = np.load(d2.save_fields_sequence(tmp_path, mesh.nodes_xy, out.results))
+    assert seq["u_nodal"].shape == (2, mesh.nodes_xy.shape[0], 2)
+    assert seq["discrepancy_ref"].shape == (2, H, W)
+    assert np.array_equal(seq["u_nodal"][1], np.asarray(out.results[1].u_nodal))
