@@ -963,6 +963,21 @@ __device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int
     }
 }
 
+// The active list (n_active = na <= FCACHE) with its prefix sums and each frame's candidate
+// rule, copied into the block's shared memory (whole block).
+__device__ void load_list(Ctl &C, int na, int *s_cpre, int *s_gpre, int *s_act, FInfo *s_fi) {
+    if (na > FCACHE) return;
+    for (int s = threadIdx.x; s <= na; s += NT) {
+        s_cpre[s] = __ldcg(C.cpre + s);
+        s_gpre[s] = __ldcg(C.gpre + s);
+    }
+    for (int s = threadIdx.x; s < na; s += NT) {
+        const int f = __ldcg(C.active + s);
+        s_act[s] = f;
+        s_fi[s] = frame_info(C.fs + f);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the persistent kernel
 // ---------------------------------------------------------------------------
@@ -976,6 +991,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     __shared__ int s_gpre[FCACHE + 1];
     __shared__ int s_act[FCACHE];
     __shared__ FInfo s_fi[FCACHE];
+    __shared__ int s_hdr[4];                         // n_active, total_chunks, total_groups, abort
     // per warp: two record buffers, then two coefficient-tile buffers (all 128-byte aligned)
     extern __shared__ __align__(128) unsigned char s_dyn[];
     Ctl C = make_ctl(ctl_base, n_frames);
@@ -1041,12 +1057,23 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             }
     }
     if (!grid_barrier(C.h, [&] { r_init(frames, n_frames, C); })) goto finish;
+    // The block's copy of the round state: the header, and for up to FCACHE active frames the
+    // active list with its prefix sums and each frame's candidate rule.
+    if (threadIdx.x == 0) {
+        s_hdr[0] = ld_vol(&C.h->n_active);
+        s_hdr[1] = ld_vol(&C.h->total_chunks);
+        s_hdr[2] = ld_vol(&C.h->total_groups);
+        s_hdr[3] = ld_vol(&C.h->abort);
+    }
+    __syncthreads();
+    load_list(C, s_hdr[0], s_cpre, s_gpre, s_act, s_fi);
+    __syncthreads();
 
     while (round < max_rounds) {                    // a slice: at most max_rounds rounds, state kept in HBM
-        const int na = ld_vol(&C.h->n_active);
-        const int total = ld_vol(&C.h->total_chunks);
-        const int tg = ld_vol(&C.h->total_groups);
-        if (na == 0) break;
+        const int na = s_hdr[0];
+        const int total = s_hdr[1];
+        const int tg = s_hdr[2];
+        if (na == 0 || s_hdr[3]) break;
         const bool trr = tr && round < trace_rounds;
         if (trr) trace[7 * round + 0] = gtimer();
         // the active list only shrinks within a launch: the same count means the same list
@@ -1067,18 +1094,6 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         // ---- P phase: chunks of the active list spread over the warps (see below) ----
         {
             const bool cached = na <= FCACHE;
-            if (cached) {
-                for (int s = threadIdx.x; s <= na; s += NT) {
-                    s_cpre[s] = __ldcg(C.cpre + s);
-                    s_gpre[s] = __ldcg(C.gpre + s);
-                }
-                for (int s = threadIdx.x; s < na; s += NT) {
-                    const int f = __ldcg(C.active + s);
-                    s_act[s] = f;
-                    s_fi[s] = frame_info(C.fs + f);
-                }
-            }
-            __syncthreads();
             const int gw = (int)((blockIdx.x * NT + threadIdx.x) >> 5);
             const int nw = (int)((gridDim.x * NT) >> 5);
             int cur = 0;   // active slot of the last located chunk (chunks ascend per warp)
@@ -1367,13 +1382,27 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                         atomicExch(&C.h->abort, 1);
                         break;
                     }
-                    __nanosleep(64);
+                    __nanosleep(32);
                 }
             }
             __threadfence();
         }
         __syncthreads();
-        if (ld_vol(&C.h->abort)) break;
+        // one round trip for the next round's state: the header (thread 0) and, for the list as it
+        // was, each frame's candidate rule; a changed list (a frame finished) is reloaded
+        if (threadIdx.x == 0) {
+            s_hdr[0] = ld_vol(&C.h->n_active);
+            s_hdr[1] = ld_vol(&C.h->total_chunks);
+            s_hdr[2] = ld_vol(&C.h->total_groups);
+            s_hdr[3] = ld_vol(&C.h->abort);
+        }
+        if (na <= FCACHE)
+            for (int s = threadIdx.x; s < na; s += NT) s_fi[s] = frame_info(C.fs + s_act[s]);
+        __syncthreads();
+        if (s_hdr[0] != na && s_hdr[0] > 0 && !s_hdr[3]) {
+            load_list(C, s_hdr[0], s_cpre, s_gpre, s_act, s_fi);
+            __syncthreads();
+        }
         if (trr) trace[7 * round + 5] = gtimer();
         ++round;
     }
