@@ -306,7 +306,8 @@ constexpr int WARP_SMEM = 2 * CHUNK_BYTES + 2 * TILE_BYTES;
 constexpr int TILE_MARGIN = 2;
 constexpr int TILE_NONE = (int)0x80008000u;                 // no valid origin (col = row = -32768)
 constexpr unsigned long long TMA_WAIT_NS = 200ull * 1000ull * 1000ull;
-constexpr int FCACHE = 64;    // active frames whose per-round lookup data is kept in shared memory
+constexpr int FCACHE = 64;
+constexpr int CAND_N = 12;    // candidate copies per staged chunk (lanes 0..11)    // active frames whose per-round lookup data is kept in shared memory
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -330,6 +331,17 @@ __device__ __forceinline__ void tensor_load_2d(void *dst, const void *map, int x
             "r"(smem_addr(dst)),
         "l"(map), "r"(x), "r"(y), "r"(smem_addr(b))
         : "memory");
+}
+// 8-byte asynchronous copy global -> shared (no register holds the value); the mbarrier's
+// pending count is decremented when this thread's earlier cp.async copies have completed
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_arrive(unsigned long long *b) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(b)) : "memory");
 }
 __device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity) {
     unsigned ok;
@@ -375,11 +387,6 @@ __device__ __forceinline__ ChunkMeta load_meta(const d2ic_frame_t *frames, int f
     }
     return m;
 }
-
-// raw candidate inputs of a chunk's nodes (lanes 0..3), combined when the chunk is processed
-struct CandRaw {
-    float2 u, g, d;
-};
 
 // Where a chunk's records and coefficient tile come from in this pass.
 struct Stage {
@@ -987,6 +994,9 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                                                    double *J_out, float *grad_out, unsigned long long *trace,
                                                    int trace_rounds, int max_rounds) {
     __shared__ unsigned long long s_bar[NWARP][2];   // per-warp mbarriers of the two record buffers
+    // per warp and buffer: the nodal candidate inputs of the staged chunk, u of node a at [a], g at
+    // [4 + a], the previous direction at [8 + a] (cp.async, completing on the buffer's mbarrier)
+    __shared__ __align__(16) float2 s_cand[NWARP][2][CAND_N];
     __shared__ int s_cpre[FCACHE + 1];               // per-round copies of the active list (na <= FCACHE)
     __shared__ int s_gpre[FCACHE + 1];
     __shared__ int s_act[FCACHE];
@@ -999,8 +1009,8 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     unsigned char *wbuf = s_dyn + (size_t)wid * WARP_SMEM;
     unsigned pipe_i = 0;   // chunks this warp has staged: buffer i & 1, completion parity (i >> 1) & 1
     if (lane == 0) {
-        mbar_init(&s_bar[wid][0], 1);
-        mbar_init(&s_bar[wid][1], 1);
+        mbar_init(&s_bar[wid][0], 1 + CAND_N);   // lane 0's expect_tx + one per candidate copy
+        mbar_init(&s_bar[wid][1], 1 + CAND_N);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     // descriptors (and their tensor maps) may have been rewritten since the previous launch
@@ -1079,6 +1089,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         // the active list only shrinks within a launch: the same count means the same list
         const bool pf_use = pf && na == pf_na && total == pf_total;
         if (pf && !pf_use) {
+            if (lane < CAND_N) mbar_arrive(&s_bar[wid][pipe_i & 1]);   // no candidates for the dropped chunk
             if (!mbar_wait(&s_bar[wid][pipe_i & 1], (pipe_i >> 1) & 1u) && lane == 0) {   // bounded
                 C.h->err = D2IC_WAIT_TIMEOUT;
                 atomicExch(&C.h->abort, 1);
@@ -1143,22 +1154,20 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 }
                 return st;
             };
-            auto load_cand = [&](const ChunkMeta &m, CandRaw &cr) {
-                if (lane < 4) {
+            // the chunk's nodal candidate inputs into s_cand (lane 4 k + a copies array k of node a),
+            // counted on the chunk's mbarrier
+            auto load_cand = [&](const ChunkMeta &m, unsigned i) {
+                const int a = lane & 3, k = lane >> 2;
+                const int nd = __shfl_sync(0xffffffffu, m.nd, a);
+                if (lane < CAND_N) {
                     const d2ic_frame_t &F = frames[m.f];
                     const FInfo fi = cached ? s_fi[m.s] : frame_info(C.fs + m.f);
-                    cr.u = __ldcg(nbuf(F, fi.iu) + m.nd);
-                    cr.g = fi.mode != 0 ? __ldcg(nbuf(F, 2 + fi.igc) + m.nd) : make_float2(0.f, 0.f);
-                    cr.d = fi.mode == 1 ? __ldcg(nbuf(F, 5 + fi.idp) + m.nd) : make_float2(0.f, 0.f);
+                    const int j = k == 0 ? fi.iu : (k == 1 ? 2 + fi.igc : 5 + fi.idp);
+                    cp_async8(&s_cand[wid][i & 1][lane], nbuf(F, j) + nd);
+                    cp_async_arrive(&s_bar[wid][i & 1]);
                 }
             };
-            auto issue = [&](const ChunkMeta &m, unsigned i, CandRaw &cr) {
-                const Stage st = issue_tma(m, i);
-                load_cand(m, cr);
-                return st;
-            };
             ChunkMeta m0{}, m1{}, m2{};
-            CandRaw r0{}, r1{};
             Stage st0{}, st1{};
             bool p_ok = true;
             // One frame: warp gw takes the contiguous chunk range [cb, ce) (neighbouring elements
@@ -1187,17 +1196,20 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                     m0 = pm0;
                     st0 = pst0;
                     m1 = pm1;
-                    load_cand(m0, r0);
                 } else {
                     m0 = fetch_meta(cb);
-                    st0 = issue(m0, pipe_i, r0);
+                    st0 = issue_tma(m0, pipe_i);
                     if (cb + cs < ce) m1 = fetch_meta(cb + cs);
                 }
+                load_cand(m0, pipe_i);
             }
             for (int g = cb; g < ce; g += cs) {
                 const bool has1 = g + cs < ce;
                 if (g + 2 * cs < ce) m2 = fetch_meta(g + 2 * cs);
-                if (has1) st1 = issue(m1, pipe_i + 1, r1);
+                if (has1) {
+                    st1 = issue_tma(m1, pipe_i + 1);
+                    load_cand(m1, pipe_i + 1);
+                }
                 const bool got = mbar_wait(&s_bar[wid][pipe_i & 1], (pipe_i >> 1) & 1u);
                 if (!__all_sync(0xffffffffu, got)) {
                     if (lane == 0) {
@@ -1211,8 +1223,9 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 float2 uc = make_float2(0.f, 0.f);
                 if (lane < 4) {
                     const FInfo fi = cached ? s_fi[m0.s] : frame_info(C.fs + m0.f);
+                    const float2 *sc = s_cand[wid][pipe_i & 1];
                     float2 dir;
-                    uc = cand_value(r0.u, r0.g, r0.d, fi.alpha, fi.beta, fi.mode, dir);
+                    uc = cand_value(sc[lane], sc[4 + lane], sc[8 + lane], fi.alpha, fi.beta, fi.mode, dir);
                 }
                 chunk_compute<KIND>(frames[m0.f], m0, uc, st0,
                                     reinterpret_cast<const uint4 *>(wbuf + (pipe_i & 1) * CHUNK_BYTES),
@@ -1220,7 +1233,6 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                                     lane);
                 ++pipe_i;
                 m0 = m1;
-                r0 = r1;
                 st0 = st1;
                 m1 = m2;
             }
@@ -1407,7 +1419,10 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         ++round;
     }
 
-    if (pf) mbar_wait(&s_bar[wid][pipe_i & 1], (pipe_i >> 1) & 1u);   // no copy in flight at exit (bounded)
+    if (pf) {                                       // no copy in flight at exit (bounded wait)
+        if (lane < CAND_N) mbar_arrive(&s_bar[wid][pipe_i & 1]);
+        mbar_wait(&s_bar[wid][pipe_i & 1], (pipe_i >> 1) & 1u);
+    }
 
 finish:
     // ---- outputs of frames that finished in this launch; running frames report D2IC_RUNNING ----
