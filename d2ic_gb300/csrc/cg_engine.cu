@@ -988,7 +988,10 @@ __device__ void load_list(Ctl &C, int na, int *s_cpre, int *s_gpre, int *s_act, 
 // ---------------------------------------------------------------------------
 // the persistent kernel
 // ---------------------------------------------------------------------------
-template <int KIND>
+// ONE: a launch of exactly one frame; the pixel pass then reads that frame's descriptor at a
+// fixed address, so its fields are loop invariants (loaded once, not per chunk; measured 2-5%
+// faster per round).
+template <int KIND, bool ONE = false>
 __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
                                                    char *ctl_base, int eval_only, const float *u_eval,
                                                    double *J_out, float *grad_out, unsigned long long *trace,
@@ -1127,7 +1130,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             // stage a chunk: TMA bulk copy of its records, 2-D TMA copy of its coefficient tile,
             // loads of its nodal candidate inputs
             auto issue_tma = [&](const ChunkMeta &m, unsigned i) {
-                const d2ic_frame_t &F = frames[m.f];
+                const d2ic_frame_t &F = frames[ONE ? 0 : m.f];
                 const int n = max(m.pe - m.pb, 0);
                 const unsigned bytes = (unsigned)min(n, D2IC_CHUNK_MAX) * 16u;
                 const uint4 *src = reinterpret_cast<const uint4 *>(F.pix) + m.pb;
@@ -1160,7 +1163,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 const int a = lane & 3, k = lane >> 2;
                 const int nd = __shfl_sync(0xffffffffu, m.nd, a);
                 if (lane < CAND_N) {
-                    const d2ic_frame_t &F = frames[m.f];
+                    const d2ic_frame_t &F = frames[ONE ? 0 : m.f];
                     const FInfo fi = cached ? s_fi[m.s] : frame_info(C.fs + m.f);
                     const int j = k == 0 ? fi.iu : (k == 1 ? 2 + fi.igc : 5 + fi.idp);
                     cp_async8(&s_cand[wid][i & 1][lane], nbuf(F, j) + nd);
@@ -1227,7 +1230,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                     float2 dir;
                     uc = cand_value(sc[lane], sc[4 + lane], sc[8 + lane], fi.alpha, fi.beta, fi.mode, dir);
                 }
-                chunk_compute<KIND>(frames[m0.f], m0, uc, st0,
+                chunk_compute<KIND>(frames[ONE ? 0 : m0.f], m0, uc, st0,
                                     reinterpret_cast<const uint4 *>(wbuf + (pipe_i & 1) * CHUNK_BYTES),
                                     reinterpret_cast<const float *>(wbuf + 2 * CHUNK_BYTES + (pipe_i & 1) * TILE_BYTES),
                                     lane);
@@ -1464,7 +1467,15 @@ template <int KIND>
 static cudaError_t occupancy(int *blocks_per_sm) {
     cudaError_t e = cudaFuncSetAttribute(cg_engine<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ENGINE_SMEM);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, cg_engine<KIND>, NT, ENGINE_SMEM);
+    e = cudaFuncSetAttribute(cg_engine<KIND, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ENGINE_SMEM);
+    if (e != cudaSuccess) return e;
+    int one = 0;   // the one-frame instance must fit as many blocks as the general one
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&one, cg_engine<KIND, true>, NT, ENGINE_SMEM);
+    if (e != cudaSuccess) return e;
+    int many = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&many, cg_engine<KIND>, NT, ENGINE_SMEM);
+    *blocks_per_sm = one < many ? one : many;
+    return e;
 }
 
 struct DevInfo {
@@ -1526,12 +1537,17 @@ static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    const bool one = n_frames == 1;
     if (kind == D2IC_INTERP_CUBIC)
-        e = cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_CUBIC>, frames, n_frames, cb, eval_only, u_eval, J_out,
-                               grad_out, trace, trace_rounds, max_rounds);
+        e = one ? cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_CUBIC, true>, frames, n_frames, cb, eval_only, u_eval,
+                                     J_out, grad_out, trace, trace_rounds, max_rounds)
+                : cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_CUBIC>, frames, n_frames, cb, eval_only, u_eval, J_out,
+                                     grad_out, trace, trace_rounds, max_rounds);
     else
-        e = cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_LINEAR>, frames, n_frames, cb, eval_only, u_eval, J_out,
-                               grad_out, trace, trace_rounds, max_rounds);
+        e = one ? cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_LINEAR, true>, frames, n_frames, cb, eval_only,
+                                     u_eval, J_out, grad_out, trace, trace_rounds, max_rounds)
+                : cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_LINEAR>, frames, n_frames, cb, eval_only, u_eval,
+                                     J_out, grad_out, trace, trace_rounds, max_rounds);
     if (e != cudaSuccess) return cuda_status(e, "cooperative launch of cg_engine");
     return D2IC_OK;
 }
