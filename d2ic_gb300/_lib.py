@@ -90,6 +90,7 @@ _SIGS = {
     "d2ic_discrepancy_map": (i32, [vp, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),
     "d2ic_central_gradient": (i32, [vp, i32, i32, vp, vp, vp]),
     "d2ic_local_coordinates": (i32, [vp, vp, vp, ctypes.c_longlong, i32, vp, vp, vp]),
+    "d2ic_structured_assign": (i32, [vp, ctypes.c_longlong, vp, i32, vp, i32, vp, vp, vp]),
     "d2ic_pcg_work_bytes": (szt, [i32, i32, i32]),
     "d2ic_pcg_solve": (i32, [vp, i32, i32, i32, vp, f32, f32, vp, vp, vp, vp, i32, f64, i32, vp, szt, vp, vp]),
     "d2ic_local_gn_slot_bytes": (szt, [i32, i32]),

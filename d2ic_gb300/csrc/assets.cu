@@ -1,6 +1,7 @@
-// Pixel-asset setup on the device: local (xi, eta) coordinates of every pixel in
-// its Q4 element by Newton's method (d2ic/pixel_assets.py:277-294, the
-// reference's _newton_quadrature), in FP64.
+// Pixel-asset setup on the device: the element of every pixel on a tensor-grid
+// mesh (d2ic/pixel_assets.py:135-237 for the grids mask_to_mesh builds), and the
+// local (xi, eta) coordinates of every pixel in its Q4 element by Newton's method
+// (d2ic/pixel_assets.py:277-294, the reference's _newton_quadrature), in FP64.
 //
 // Each step is the host restatement's operation sequence with correctly rounded
 // FP64 intrinsics (no contraction into FMAs): shape functions and derivatives,
@@ -59,9 +60,59 @@ __global__ void __launch_bounds__(256) local_coords_kernel(const double *__restr
     }
 }
 
+// number of entries of the ascending array g[0..n) that are <= x (searchsorted, side "right")
+__device__ __forceinline__ int count_le(const double *g, int n, double x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (g[mid] <= x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The four cells around the pixel whose closed rectangles can hold it (the last grid line <= x
+// and the one before, likewise in y); the lowest element index among those that do.
+__global__ void __launch_bounds__(256) structured_assign_kernel(const double *__restrict__ pc, long long n,
+                                                                const double *__restrict__ gx, int nx,
+                                                                const double *__restrict__ gy, int ny,
+                                                                const long long *__restrict__ cell,
+                                                                long long *__restrict__ elts) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        const double x = pc[2 * p], y = pc[2 * p + 1];
+        const int ixr = count_le(gx, nx, x) - 1, iyr = count_le(gy, ny, y) - 1;
+        long long best = -1;
+        for (int dx = 0; dx < 2; ++dx) {
+            const int cx = ixr - dx;
+            if (cx < 0 || cx > nx - 2 || !(gx[cx] <= x && x <= gx[cx + 1])) continue;
+            for (int dy = 0; dy < 2; ++dy) {
+                const int cy = iyr - dy;
+                if (cy < 0 || cy > ny - 2 || !(gy[cy] <= y && y <= gy[cy + 1])) continue;
+                const long long e = cell[(long long)cy * (nx - 1) + cx];
+                if (e >= 0 && (best < 0 || e < best)) best = e;
+            }
+        }
+        elts[p] = best;
+    }
+}
+
 }  // namespace d2ic
 
 using namespace d2ic;
+
+extern "C" int d2ic_structured_assign(const double *pixel_coords, long long n_pix, const double *gx, int nx,
+                                      const double *gy, int ny, const long long *cell, long long *elts,
+                                      void *stream) {
+    D2IC_REQUIRE(n_pix >= 0 && nx >= 2 && ny >= 2, "d2ic_structured_assign: bad sizes");
+    if (n_pix == 0) return D2IC_OK;
+    D2IC_REQUIRE(pixel_coords && gx && gy && cell && elts, "d2ic_structured_assign: null pointer");
+    long long blocks = (n_pix + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    structured_assign_kernel<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(pixel_coords, n_pix, gx, nx, gy, ny, cell,
+                                                                            elts);
+    D2IC_CHECK_LAUNCH("structured_assign_kernel");
+    return D2IC_OK;
+}
 
 extern "C" int d2ic_local_coordinates(const double *pixel_coords, const int *pixel_nodes, const double *nodes,
                                       long long n_pix, int iters, double *xi, double *eta, void *stream) {

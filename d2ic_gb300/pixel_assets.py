@@ -157,6 +157,39 @@ def build_pixel_to_element_mapping_numpy(pixel_coords, nodes_coord, elements, ch
     return elts, pn
 
 
+def structured_assign_device(pc: np.ndarray, gx, gy, cell, device=None) -> np.ndarray:
+    """:func:`_structured_assign` on the GPU (``d2ic_structured_assign``): the same FP64
+    comparisons, so the element map is identical."""
+    import torch
+
+    from . import _lib
+    from ._lib import ptr
+    dev = torch.device(device if device is not None else "cuda")
+    n = int(pc.shape[0])
+    if n == 0:
+        return np.zeros((0,), dtype=np.int64)
+    t_pc = torch.from_numpy(np.ascontiguousarray(pc, dtype=np.float64)).to(dev)
+    t_gx = torch.from_numpy(np.ascontiguousarray(gx, dtype=np.float64)).to(dev)
+    t_gy = torch.from_numpy(np.ascontiguousarray(gy, dtype=np.float64)).to(dev)
+    t_cell = torch.from_numpy(np.ascontiguousarray(cell, dtype=np.int64)).to(dev)
+    out = torch.empty(n, dtype=torch.int64, device=dev)
+    _lib.call("d2ic_structured_assign", ptr(t_pc), n, ptr(t_gx), int(gx.size), ptr(t_gy), int(gy.size), ptr(t_cell),
+              ptr(out), _lib.stream_handle())
+    return out.cpu().numpy()
+
+
+def _pixel_elements(pc: np.ndarray, nodes: np.ndarray, el: np.ndarray):
+    """``build_pixel_to_element_mapping_numpy`` with the tensor-grid search on the GPU when one
+    is present (identical results)."""
+    if pc.shape[0] > 0 and el.size > 0 and _gpu_available():
+        sg = structured_grid(nodes, el)
+        if sg is not None:
+            elts = structured_assign_device(pc, *sg)
+            pn = np.where((elts >= 0)[:, None], el[np.maximum(elts, 0)], 0)
+            return elts, pn
+    return build_pixel_to_element_mapping_numpy(pc, nodes, el)
+
+
 def _solve2(a11, a12, a21, a22, b1, b2):
     # LU with partial pivoting on a 2x2 system (row swap when |a21| > |a11|)
     swap = np.abs(a21) > np.abs(a11)
@@ -335,7 +368,9 @@ def build_pixel_assets(mesh: Mesh, ref_image, binning: float, roi_mask=None, bbo
         rows = np.clip(np.floor(pc[:, 1] - 0.5).astype(int), 0, H - 1)
         cols = np.clip(np.floor(pc[:, 0] - 0.5).astype(int), 0, W - 1)
         pc = pc[roi_mask[rows, cols]]
-    elts, pn = build_pixel_to_element_mapping_numpy(pc, nodes, elements, chunk_size=chunk_size)
+    if chunk_size < 1:
+        raise ValueError("chunk_size must be >= 1")
+    elts, pn = _pixel_elements(pc, nodes, elements)
     keep = elts >= 0
     pc, pn, elts = pc[keep], pn[keep], elts[keep]
     N, xe = compute_pixel_shape_functions(pc, pn, nodes)

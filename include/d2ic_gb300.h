@@ -172,6 +172,17 @@ D2IC_API int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n_n
 D2IC_API int d2ic_local_coordinates(const double *pixel_coords, const int *pixel_nodes, const double *nodes,
                                     long long n_pix, int iters, double *xi, double *eta, void *stream);
 
+/* Element of each pixel on a tensor-grid mesh of axis-aligned cells (the
+ * pixel-to-element map of build_pixel_assets, d2ic/pixel_assets.py:135-237, for
+ * the grids mask_to_mesh builds): the lowest element index whose closed cell
+ * rectangle contains the pixel centre, -1 if none.  pixel_coords: 2 * n_pix (x, y);
+ * gx: nx ascending grid columns; gy: ny ascending grid rows; cell: (ny - 1) *
+ * (nx - 1) element index per cell, row-major, -1 for no element; elts: n_pix.
+ * FP64 comparisons only, so the result equals the host search exactly.  Device
+ * pointers. */
+D2IC_API int d2ic_structured_assign(const double *pixel_coords, long long n_pix, const double *gx, int nx,
+                                    const double *gy, int ny, const long long *cell, long long *elts, void *stream);
+
 /* ---- local Gauss-Newton refinement (replaces LocalGaussNewtonSolver,
  *      d2ic/solver_local_gn.py:34-414) ---- */
 

@@ -75,3 +75,34 @@ def test_device_local_coordinates_bit_exact(cuda):
     xh, eh = local_coordinates(pc, pn, nodes)
     xd, ed = local_coordinates_device(pc, pn, nodes, device=cuda)
     assert np.array_equal(xh.view(np.int64), xd.view(np.int64)) and np.array_equal(eh.view(np.int64), ed.view(np.int64))
+
+
+def test_device_structured_assign_exact(cuda):
+    """GPU tensor-grid pixel -> element search == host search, including pixels on grid lines
+    (shared edges: lowest element wins), in holes and outside the grid."""
+    import d2ic_gb300 as d2
+    from d2ic_gb300.pixel_assets import _structured_assign, structured_assign_device, structured_grid
+    from d2ic_gb300.synthetic import ellipse_mask
+    H = W = 256
+    mask = ellipse_mask(H, W, np.random.default_rng(3))
+    mesh, _ = d2.mask_to_mesh_assets(mask, 12)
+    nodes = np.asarray(mesh.nodes_xy, np.float64)
+    sg = structured_grid(nodes, np.asarray(mesh.elements, np.int64))
+    assert sg is not None
+    gx, gy, _cell = sg
+    rng = np.random.default_rng(4)
+    pc = np.concatenate([
+        rng.uniform(-5, W + 5, (20000, 2)),                                   # anywhere, also outside
+        np.stack([rng.choice(gx, 4000), rng.uniform(0, H, 4000)], 1),        # on vertical grid lines
+        np.stack([rng.uniform(0, W, 4000), rng.choice(gy, 4000)], 1),        # on horizontal grid lines
+        np.stack([rng.choice(gx, 2000), rng.choice(gy, 2000)], 1),           # on grid nodes
+    ])
+    host = _structured_assign(pc, *sg)
+    dev = structured_assign_device(pc, *sg, device=cuda)
+    assert (host >= 0).sum() > 10000 and (host < 0).sum() > 1000
+    assert np.array_equal(host, dev)
+    # and through build_pixel_assets (device path) against the host mapping function
+    ref = rng.random((H, W)).astype(np.float32)
+    pix = d2.build_pixel_assets(mesh, ref, 1.0)
+    elts, _ = d2.pixel_assets.build_pixel_to_element_mapping_numpy(pix.pixel_coords_ref, nodes, mesh.elements)
+    assert np.array_equal(elts, pix.pixel_elts)
