@@ -1,27 +1,28 @@
 // Persistent cooperative nonlinear-CG engine for the global FE-DIC objective.
 //
 // One launch solves a batch of independent frames (the plain GlobalCGSolver
-// drop-in is a batch of one).  All frames advance in lock-step "rounds"; one
-// round evaluates, for every active frame, the objective and its gradient at
-// the frame's current candidate point:
+// drop-in is a batch of one, run by a one-frame instance of the kernel).  All
+// frames advance in lock-step "rounds"; one round evaluates, for every active
+// frame, the objective and its gradient at the frame's current candidate point:
 //
-//   P phase  (pixels)  each warp takes chunks (<= 256 pixels of one element)
-//                      and computes, for the candidate u_c = u + alpha * dir,
-//                        r = I2(x + sum_a N_a u_c[a]) - I1,
-//                      the chunk's sum r^2 (FP64) and its 8 nodal gradient
-//                      partials sum r * dI2/dx * N_a (FP32).  No atomics on data.
-//   barrier
-//   N phase  (nodes)   per node: gather its chunk partials (node->chunk CSR),
-//                      add the spring gradient over the neighbour table,
-//                      write the trial gradient, trial point and trial
-//                      direction; per group of 512 nodes reduce (FP64, fixed
-//                      order) sum r^2, spring energy, g.g, g.(g - g_cur),
-//                      g_cur.dir.
-//   barrier + R        the last block to arrive reduces the group partials of
-//                      each frame (fixed order) and runs the CG control of
-//                      d2ic/solver_global_cg.py:362-461 (stop test, PR+ beta,
-//                      restart on g.d >= 0, Armijo with 10 halvings and the
-//                      forced 2^-10 step), then rebuilds the active list.
+//   pixel pass   each warp takes chunks (<= 256 pixels of one element) and
+//                computes, for the candidate u_c = u + alpha * dir,
+//                  r = I2(x + sum_a N_a u_c[a]) - I1,
+//                the chunk's sum r^2 (double-float) and its 8 nodal gradient
+//                partials sum r * dI2/dx * N_a (FP32), written to the chunk's
+//                own node slots; then it counts its chunks into the node
+//                groups (32 nodes) they touch.  No atomics on data.
+//   node work    the warp that owns a group waits (bounded) until every chunk
+//                of the group has counted, gathers each node's slots, adds the
+//                spring gradient over the neighbour table, writes the trial
+//                gradient, point and direction, and reduces (fixed order) sum
+//                r^2, spring energy, g.g, g.(g - g_cur), g_cur.dir; the warp
+//                that completes a supergroup of 32 groups reduces it, and the
+//                warp that completes a frame's last supergroup runs the CG
+//                control of d2ic/solver_global_cg.py:362-461 (stop test, PR+
+//                beta, restart on g.d >= 0, Armijo with 10 halvings and the
+//                forced 2^-10 step); the frame's round counter releases the
+//                next round.
 //
 // Because every partial is written to its own slot and reduced in an order
 // fixed by the frame's own data layout, a frame's result does not depend on
@@ -31,9 +32,10 @@
 // that evaluated it, so an iteration costs one pixel pass per line-search
 // trial (the reference's separate value_and_grad pass is not repeated).
 //
-// Grid barriers are the engine's own (atomic counter + generation word) with a
-// globaltimer-bounded wait: a block that waits longer than D2IC_WAIT_NS sets
-// an abort flag and every block leaves the kernel at its next barrier.
+// Every wait is bounded by the globaltimer (the launch's grid barrier, the group
+// and round waits: WAIT_NS; the TMA/cp.async completions: TMA_WAIT_NS): a warp
+// that waits longer sets D2IC_WAIT_TIMEOUT and an abort flag, drains its own
+// copies and every block leaves the kernel.
 #include <cuda.h>   // CUtensorMap and its enums (the encoder is fetched from the driver at run time)
 #include <stddef.h>
 #include <string.h>
@@ -284,15 +286,16 @@ __device__ __forceinline__ int find_slot_smem(const int *pre, int n, int x) {
 // ---------------------------------------------------------------------------
 // P phase: one chunk per warp, software-pipelined
 // ---------------------------------------------------------------------------
-// Each warp walks its chunks (c, c + W, c + 2W, ... for W warps in the grid)
-// with three stages in flight:
+// Each warp walks its chunks (a contiguous range for one frame, c, c + W,
+// c + 2W, ... for W warps in the grid with several) with three stages in flight:
 //   chunk i + 2: metadata (pixel range, nodes, slots) loaded into registers;
 //   chunk i + 1: pixel records copied into the warp's shared-memory buffer by
 //                one TMA bulk copy (cp.async.bulk, completion on an mbarrier),
-//                nodal candidate inputs (u, g, d) loaded into registers;
+//                nodal candidate inputs (u, g, d) copied by cp.async onto the
+//                same mbarrier;
 //   chunk i:     sampled and reduced.
 // A warp therefore never waits on a metadata -> records / candidates round
-// trip; only the coefficient taps are read on demand (L1 captures their reuse).
+// trip.
 // Each chunk also stages its window of the deformed image's coefficients
 // (tile_w x tile_h floats) with a 2-D TMA copy on the same mbarrier.  The
 // window is placed from the chunk's candidate of the previous pass, with a
@@ -1127,8 +1130,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 m.s = s;
                 return m;
             };
-            // stage a chunk: TMA bulk copy of its records, 2-D TMA copy of its coefficient tile,
-            // loads of its nodal candidate inputs
+            // stage a chunk: TMA bulk copy of its records, 2-D TMA copy of its coefficient tile
             auto issue_tma = [&](const ChunkMeta &m, unsigned i) {
                 const d2ic_frame_t &F = frames[ONE ? 0 : m.f];
                 const int n = max(m.pe - m.pb, 0);
