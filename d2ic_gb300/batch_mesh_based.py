@@ -19,7 +19,7 @@ from .dataclasses import BatchConfig, BatchDiagnostics, BatchResult, DICResult
 from .dic_mesh_based import DICMeshBased
 from .mesh_assets import MeshAssets
 from .outputs import save_frame_npz
-from .propagators import DisplacementPropagatorBase
+from .propagators import ConstantVelocityPropagator, DisplacementPropagatorBase, PreviousDisplacementPropagator
 from .types import Array
 
 
@@ -126,6 +126,11 @@ class BatchMeshBased(BatchBase):
         except TypeError:
             n_frames = None
         per_frame: list[DICResult] = []
+        if self._can_pipeline():
+            self._sequence_pipelined(images, per_frame, latencies, save, out_dir, progress or verbose, n_frames)
+            diag = BatchDiagnostics(info={"stage": "batch_mesh_based", "n_frames": len(per_frame),
+                                          "warm_start_from_previous": self.config.warm_start_from_previous})
+            return BatchResult(results=per_frame, diagnostics=diag)
         u_prev = None
         u_prevprev = None
         for k, Idef in enumerate(_prefetched(images)):
@@ -154,6 +159,64 @@ class BatchMeshBased(BatchBase):
         diag = BatchDiagnostics(info={"stage": "batch_mesh_based", "n_frames": len(per_frame),
                                       "warm_start_from_previous": self.config.warm_start_from_previous})
         return BatchResult(results=per_frame, diagnostics=diag)
+
+    def _can_pipeline(self) -> bool:
+        """Frames can overlap (frame k + 1 queued before frame k is collected) when the CG driver
+        splits its runs, no local refinement is chained, the propagator is one of the built-in
+        rules (they work on device tensors) and a GPU is present."""
+        import torch
+        if self.dic_local is not None or not hasattr(self.dic_mesh, "run_begin"):
+            return False
+        if not hasattr(getattr(self.dic_mesh, "solver", None), "solve_begin"):
+            return False
+        if self.propagator is not None and type(self.propagator) not in (PreviousDisplacementPropagator,
+                                                                         ConstantVelocityPropagator):
+            return False
+        return torch.cuda.is_available()
+
+    def _sequence_pipelined(self, images, per_frame, latencies, save, out_dir, talk, n_frames):
+        """The per-frame loop with frame k + 1 queued before frame k's results are collected, so
+        the host work of a frame (copies out, result objects, files) overlaps the next solve.
+        Warm starts use device copies of the previous solutions: the same values as the host
+        path, so the results are identical."""
+        import time
+        u_prev = u_prevprev = None
+        pending = None
+        done = [0.0]   # when the previous frame's results were collected
+
+        def collect(item):
+            # a frame's latency runs from when its solve could start (queued, and the previous
+            # frame done) to its results on the host: the service time, without the wait behind
+            # the previous frame that queueing ahead adds
+            k, pend, t0 = item
+            res = self.dic_mesh.run_end(pend)
+            now = time.perf_counter()
+            per_frame.append(res)
+            if latencies is not None:
+                latencies.append(now - max(t0, done[0]))
+            done[0] = now
+            if save:
+                save_frame_npz(out_dir / f"frame_{k:04d}.npz", res)
+            if talk:
+                print(f"[Batch] Frame {k + 1}{'' if n_frames is None else '/' + str(n_frames)}: done")
+
+        for k, Idef in enumerate(_prefetched(images)):
+            t0 = time.perf_counter()
+            if talk:
+                print(f"[Batch] Frame {k + 1}{'' if n_frames is None else '/' + str(n_frames)}: start")
+            if self.propagator is not None:
+                u_warm = self.propagator.propagate(u_prev=u_prev, u_prevprev=u_prevprev)
+            else:
+                u_warm = u_prev if self.config.warm_start_from_previous else None
+            if u_warm is not None:
+                self.dic_mesh.set_initial_guess(u_warm)
+            pend = self.dic_mesh.run_begin(Idef)
+            u_prevprev, u_prev = u_prev, pend.u_device.clone()   # queued after the solve
+            if pending is not None:
+                collect(pending)
+            pending = (k, pend, t0)
+        if pending is not None:
+            collect(pending)
 
     def end(self, result: BatchResult) -> BatchResult:
         return BatchResult(results=result.results,

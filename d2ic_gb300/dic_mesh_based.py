@@ -30,6 +30,21 @@ class MeshDICState:
     u0_nodal: Array | None = None
 
 
+class _PendingFrame:
+    """A frame queued by ``DICMeshBased.run_begin``."""
+
+    def __init__(self):
+        self.handle = None
+        self.u_device = None
+        self.strain = None
+        self.strain_state = None
+        self.strain_error = None
+        self.disc_state = None
+        self.disc_map = None
+        self.disc_pending = None
+        self.event = None
+
+
 class DICMeshBased(DICBase):
     def __init__(self, mesh: Mesh, solver: SolverBase, config: MeshDICConfig) -> None:
         self.mesh = mesh
@@ -37,6 +52,8 @@ class DICMeshBased(DICBase):
         self.config = config
         self._state: MeshDICState | None = None
         self._strain_dev = None
+        self._strain_pinned = [None, None]   # per pending frame (two in flight at most)
+        self._strain_flip = 0
         self._map_layout = None
 
     def prepare(self, ref_image: Array, assets: Optional[MeshAssets] = None) -> None:
@@ -81,11 +98,86 @@ class DICMeshBased(DICBase):
         return voigt
 
     def run(self, def_image: Array) -> DICResult:
+        return self.run_end(self.run_begin(def_image))
+
+    def run_begin(self, def_image: Array):
+        """Queue one frame on the current stream -- the solve, the strain, the discrepancy map if
+        configured, and the copies of their results to pinned host memory -- without waiting, and
+        return the pending frame for :meth:`run_end`.  A sequence driver can queue frame k + 1
+        before it collects frame k, so the host work of a frame overlaps the next solve.  Solvers
+        without a split solve (``solve_begin``) run synchronously here."""
+        import torch
         if self._state is None:
             raise RuntimeError("DICMeshBased.prepare() must be called before run().")
+        begin = getattr(self.solver, "solve_begin", None)
+        if begin is None:
+            return self._run_sync(def_image)
+        assets = self._state.assets
+        pend = _PendingFrame()
+        pend.handle = begin(self._state, def_image)
+        u_dev = pend.handle.u_device
+        pend.u_device = u_dev
+        if assets.node_neighbor_index is not None and assets.node_neighbor_degree is not None:
+            try:
+                sd = self._strain(u_dev)
+                i = self._strain_flip
+                self._strain_flip ^= 1
+                if self._strain_pinned[i] is None or self._strain_pinned[i].shape != sd.shape:
+                    self._strain_pinned[i] = torch.empty(sd.shape, dtype=sd.dtype).pin_memory()
+                self._strain_pinned[i].copy_(sd, non_blocking=True)
+                pend.strain = self._strain_pinned[i]
+                pend.strain_state = "green_lagrange"
+            except Exception as exc:   # recorded, not raised (reference behaviour)
+                pend.strain_state = "failed_green_lagrange"
+                pend.strain_error = str(exc)
+        else:
+            pend.strain_state = "skipped_no_neighbors"
+        if bool(getattr(self.config, "compute_discrepancy_map", False)):
+            if assets.pixel_data is None:
+                pend.disc_state = "skipped_no_pixel_assets"
+            else:
+                pend.disc_map, pend.disc_pending = self._discrepancy(def_image, u_dev, wait=False)
+                pend.disc_state = "discrepancy_ref"
+        pend.event = torch.cuda.Event()
+        pend.event.record()
+        return pend
+
+    def run_end(self, pend) -> DICResult:
+        """Wait for a frame queued by :meth:`run_begin` and return its result."""
+        if isinstance(pend, DICResult):
+            return pend
+        from .pixel_maps import discrepancy_rms
+        pend.event.synchronize()
+        sol = self.solver.solve_end(self._state, pend.handle, wait=False)
+        u_nodal = sol.u_nodal
+        info = {"stage": "mesh_based"}
+        if getattr(sol, "n_iters", None) is not None:
+            info["n_iters"] = int(sol.n_iters)
+        if getattr(sol, "status", None) is not None:
+            info["status"] = sol.status
+        if getattr(sol, "history", None) is not None:
+            info["history"] = "attached"
+        info["strain"] = pend.strain_state
+        if pend.strain is not None:
+            strain = pend.strain.numpy().copy()
+        else:
+            strain = np.zeros((np.asarray(u_nodal).shape[0], 3), dtype=np.float32)
+            if pend.strain_error is not None:
+                info["strain_error"] = pend.strain_error
+        pixel_maps = {}
+        if pend.disc_state is not None:
+            info["discrepancy"] = pend.disc_state
+            if pend.disc_map is not None:
+                pixel_maps["discrepancy_ref"] = pend.disc_map   # kept on the device, as the reference keeps it
+                info["discrepancy_rms"] = discrepancy_rms(pend.disc_pending)
+        return DICResult(u_nodal=u_nodal, strain=strain, diagnostics=DICDiagnostics(info=info),
+                         history=getattr(sol, "history", None), pixel_maps=pixel_maps)
+
+    def _run_sync(self, def_image: Array) -> DICResult:
+        """One frame through a solver without a split solve."""
+        assets = self._state.assets
         sol = self.solver.solve(self._state, def_image)
         u_nodal = sol.u_nodal
-        assets = self._state.assets
         info = {"stage": "mesh_based"}
         if getattr(sol, "n_iters", None) is not None:
             info["n_iters"] = int(sol.n_iters)
@@ -118,10 +210,11 @@ class DICMeshBased(DICBase):
         return DICResult(u_nodal=u_nodal, strain=strain, diagnostics=DICDiagnostics(info=info),
                          history=getattr(sol, "history", None), pixel_maps=pixel_maps)
 
-    def _discrepancy(self, def_image, u):
-        """Discrepancy map through the solver's device layout (or one built for the maps)."""
+    def _discrepancy(self, def_image, u, wait: bool = True):
+        """Discrepancy map through the solver's device layout (or one built for the maps):
+        ``(map, rms)``, or ``(map, pending sums)`` with ``wait=False``."""
         from .engine import FrameSlot, descriptors_to_device
-        from .pixel_maps import discrepancy_map_ref
+        from .pixel_maps import discrepancy_map_queue, discrepancy_map_ref
         layout = getattr(self.solver, "_layout", None)
         desc = getattr(self.solver, "_desc_dev", None)
         if layout is None or desc is None:
@@ -131,4 +224,6 @@ class DICMeshBased(DICBase):
                 lay = FrameLayout(self._state.assets.pixel_data, n_nodes, self._state.ref_image, "linear")
                 self._map_layout = (lay, descriptors_to_device([FrameSlot(lay, 1).desc], lay.device))
             layout, desc = self._map_layout
+        if not wait:
+            return discrepancy_map_queue(layout, desc, def_image, u)
         return discrepancy_map_ref(layout, desc, def_image, u)

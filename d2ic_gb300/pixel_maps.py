@@ -18,6 +18,19 @@ from .engine import FrameLayout, as_device_image
 
 def discrepancy_map_ref(layout: FrameLayout, desc_dev: torch.Tensor, def_image, u, stream=None):
     """(map (H, W) float32 CUDA tensor, rms) for displacement ``u`` (Nn, 2) and a deformed image."""
+    out, pending = discrepancy_map_queue(layout, desc_dev, def_image, u, stream)
+    return out, discrepancy_rms(pending)
+
+
+def discrepancy_rms(pending) -> float:
+    """The RMS of a map queued by :func:`discrepancy_map_queue` (waits for it)."""
+    sums, cnts = pending
+    n = int(cnts.sum())
+    return float(torch.sqrt(sums.sum() / max(n, 1)))
+
+
+def discrepancy_map_queue(layout: FrameLayout, desc_dev: torch.Tensor, def_image, u, stream=None):
+    """Queue the map without waiting: (map tensor, pending partial sums for :func:`discrepancy_rms`)."""
     dev = layout.device
     ref = layout.ref_image
     dimg = as_device_image(def_image, dev)
@@ -28,6 +41,4 @@ def discrepancy_map_ref(layout: FrameLayout, desc_dev: torch.Tensor, def_image, 
     cnts = torch.zeros(nc, dtype=torch.int32, device=dev)
     _lib.call("d2ic_discrepancy_map", ptr(desc_dev), layout.n_chunks, ptr(ref), ptr(dimg), ptr(uu), layout.H,
               layout.W, ptr(out), ptr(sums), ptr(cnts), _lib.stream_handle(stream))
-    n = int(cnts.sum())
-    rms = float(torch.sqrt(sums.sum() / max(n, 1)))
-    return out, rms
+    return out, (sums, cnts)

@@ -40,6 +40,15 @@ def _normalize_interpolation(interpolation: str) -> str:
     return value
 
 
+class SolveHandle:
+    """A frame queued by ``GlobalCGSolver.solve_begin``: its device displacement and the pinned
+    buffers its results are copied into."""
+
+    def __init__(self, u_device, bufs):
+        self.u_device = u_device
+        self.bufs = bufs
+
+
 class GlobalCGSolver(SolverBase):
     """Global CG solver for mesh DIC; expects ``MeshAssets.pixel_data``."""
 
@@ -66,7 +75,9 @@ class GlobalCGSolver(SolverBase):
         self._desc_dev = None
         self._desc_params = None
         self._engine = None
-        self._pinned = None
+        self._pinned_sets = None
+        self._pinned_flip = 0
+        self._last_handle = None
 
     # -- plugin interface -------------------------------------------------------------
     def compile(self, assets: Any) -> None:
@@ -97,11 +108,14 @@ class GlobalCGSolver(SolverBase):
             self._layout_key = key
             self._desc_params = None
             nn = n_nodes
-            self._pinned = {
+            # two sets of pinned result buffers: a frame's copies may still be pending while the
+            # next frame is queued (solve_begin / solve_end)
+            self._pinned_sets = [{
                 "u": torch.empty((nn, 2), dtype=torch.float32).pin_memory(),
                 "hist": torch.empty(self._slot.hist.shape, dtype=torch.float32).pin_memory(),
                 "info": torch.empty(3, dtype=torch.int32).pin_memory(),
-            }
+            } for _ in range(2)]
+            self._pinned_flip = 0
         params = (float(state.config.tol), float(state.config.reg_strength))
         if params != self._desc_params:
             self._slot.set_params(*params)
@@ -122,17 +136,36 @@ class GlobalCGSolver(SolverBase):
         torch.cuda.synchronize(self._device)
 
     def solve(self, state: Any, def_image: Array) -> GlobalCGResult:
+        self.solve_begin(state, def_image)
+        return self.solve_end(state)
+
+    def solve_begin(self, state: Any, def_image: Array) -> "SolveHandle":
+        """Queue one frame's solve and the copies of its results on the current stream without
+        waiting.  The handle's ``u_device`` is the displacement on the device, on which more work
+        (the strain) can be queued; :meth:`solve_end` returns the result.  Two frames may be
+        pending at once (the second one's solve overwrites ``u_device``)."""
         if not self._compiled:
             raise RuntimeError("GlobalCGSolver.compile() must be called before solve().")
         slot = self._ensure(state)
         slot.load_image(def_image)
         slot.set_u0(state.u0_nodal)
         self._engine.solve(self._desc_dev, 1, self._kind, self._grid_blocks)
-        pu, ph, pi = self._pinned["u"], self._pinned["hist"], self._pinned["info"]
-        pu.copy_(slot.u_out, non_blocking=True)
-        ph.copy_(slot.hist, non_blocking=True)
-        pi.copy_(slot.info, non_blocking=True)
-        torch.cuda.current_stream(self._device).synchronize()
+        bufs = self._pinned_sets[self._pinned_flip]
+        self._pinned_flip ^= 1
+        bufs["u"].copy_(slot.u_out, non_blocking=True)
+        bufs["hist"].copy_(slot.hist, non_blocking=True)
+        bufs["info"].copy_(slot.info, non_blocking=True)
+        self._last_handle = SolveHandle(slot.u_out, bufs)
+        return self._last_handle
+
+    def solve_end(self, state: Any, handle: "SolveHandle" = None, wait: bool = True) -> GlobalCGResult:
+        """The result of a frame queued by :meth:`solve_begin` (the last one by default); with
+        ``wait=False`` the caller has already waited for its copies (an event after them)."""
+        handle = handle if handle is not None else self._last_handle
+        slot = self._slot
+        pu, ph, pi = handle.bufs["u"], handle.bufs["hist"], handle.bufs["info"]
+        if wait:
+            torch.cuda.current_stream(self._device).synchronize()
         n_iters, status = int(pi[0]), int(pi[1])
         if status in (_lib.WAIT_TIMEOUT, _lib.CUDA_ERROR):
             raise _lib.D2ICError(status, "CG engine aborted")
@@ -149,7 +182,7 @@ class GlobalCGSolver(SolverBase):
             history=ph.numpy()[: slot.max_iter].copy() if save_history else None,
             n_iters=n_iters,
             status=_lib.STATUS_NAMES.get(status, str(status)),
-            u_device=slot.u_out,
+            u_device=handle.u_device,
         )
 
     # -- diagnostics ---------------------------------------------------------------------
