@@ -23,7 +23,7 @@ import torch
 
 from . import _lib
 from ._lib import ptr
-from .engine import PAD, Engine, FrameLayout, FrameSlot, descriptors_to_device, prepare_coefficients
+from .engine import PAD, FrameLayout, FrameSlot, descriptors_to_device, prepare_coefficients
 
 
 def _pair(a, b):

@@ -12,7 +12,7 @@ from typing import Tuple
 import numpy as np
 from scipy import ndimage
 
-from .mesh_assets import Mesh, MeshAssets, compute_element_centers, make_mesh_assets
+from .mesh_assets import Mesh, MeshAssets, compute_element_centers
 
 
 def downsample_mask(mask: np.ndarray, binning: int) -> np.ndarray:

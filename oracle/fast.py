@@ -13,7 +13,7 @@ import subprocess
 
 import numpy as np
 
-from .cubic import ORACLE_PAD, bspline_coefficients, cubic_sample
+from .cubic import ORACLE_PAD, cubic_sample
 from .objective import Problem, cg_solve, reg_energy, reg_energy_grad
 
 _HERE = os.path.dirname(os.path.abspath(__file__))

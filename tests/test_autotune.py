@@ -5,7 +5,6 @@ import json
 
 import numpy as np
 import pytest
-import torch
 
 
 def _frame(H=128, elem=16, seed=5):

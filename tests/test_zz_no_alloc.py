@@ -14,7 +14,6 @@ from __future__ import annotations
 
 import ctypes
 
-import numpy as np
 import pytest
 import torch
 
