@@ -484,6 +484,7 @@ def run_adjoint(args, dev):
     R = args.adjoint_realisations
     g = torch.Generator(device=dev).manual_seed(3000)
     noise = 2.0 * torch.randn((R, H, W), generator=g, device=dev, dtype=torch.float32)
+    adj.jvp(noise, rtol=1e-6)                      # warm-up: work buffers sized for R right-hand sides
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     du = adj.jvp(noise, rtol=1e-6)
