@@ -46,8 +46,14 @@ namespace d2ic {
 
 constexpr int NT = 512;                        // threads per block
 constexpr int NWARP = NT / 32;
+static_assert(NWARP == 16, "a supergroup is the warps of one block");
 constexpr int GN = D2IC_NODE_GROUP;            // nodes per group: one per lane of the warp that reduces it
 static_assert(GN == 32, "a node group is one warp");
+// Groups per supergroup.  A frame's group range in the active list is padded to a multiple of
+// SG, so when every warp owns at most one group, supergroup sg of a frame is owned by warps
+// 0 .. SG-1 of one block and is reduced through that block's shared memory.
+constexpr int SG = 16;
+__host__ __device__ constexpr int pad_groups(int n) { return (n + SG - 1) / SG * SG; }
 #ifndef D2IC_ENGINE_MINB
 #define D2IC_ENGINE_MINB 1   // resident blocks per SM the register budget is sized for
 #endif
@@ -824,7 +830,7 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
         if (ld_vol(&C.fs[f].state) != ST_DONE) {
             ++cnt;
             ch += frames[f].n_chunks;
-            gr += frames[f].n_groups;
+            gr += pad_groups(frames[f].n_groups);
         }
     int ta, tb, tc;
     block_scan3(cnt, ch, gr, ta, tb, tc);
@@ -843,7 +849,7 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
             C.gpre[slot] = gp;
             ++slot;
             cp += frames[f].n_chunks;
-            gp += frames[f].n_groups;
+            gp += pad_groups(frames[f].n_groups);
         }
     __syncthreads();
 }
@@ -892,7 +898,7 @@ __device__ void rebuild_active_warp(const d2ic_frame_t *frames, int n_frames, Ct
         if (ld_vol(&C.fs[f].state) != ST_DONE) {
             ++cnt;
             ch += frames[f].n_chunks;
-            gr += frames[f].n_groups;
+            gr += pad_groups(frames[f].n_groups);
         }
     int ic = cnt, ih = ch, ig = gr;
 #pragma unroll
@@ -915,7 +921,7 @@ __device__ void rebuild_active_warp(const d2ic_frame_t *frames, int n_frames, Ct
             C.gpre[slot] = gp;
             ++slot;
             cp += frames[f].n_chunks;
-            gp += frames[f].n_groups;
+            gp += pad_groups(frames[f].n_groups);
         }
     if (lane == 0) {
         C.h->n_active = ta;
@@ -937,7 +943,7 @@ __device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int
     fc.alpha_reg = F.alpha_reg;
     fc.max_iter = F.max_iter;
     fc.n_pix = F.n_pix;
-    const int nsg = (F.n_groups + GN - 1) / GN;
+    const int nsg = (F.n_groups + SG - 1) / SG;
     const float2 *sp = reinterpret_cast<const float2 *>(F.group_part) + (size_t)F.n_groups * D2IC_NPART;
     for (int g = lane; g < nsg; g += 32) {
         float2 v[5];
@@ -1008,6 +1014,8 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     __shared__ int s_act[FCACHE];
     __shared__ FInfo s_fi[FCACHE];
     __shared__ int s_hdr[4];                         // n_active, total_chunks, total_groups, abort
+    __shared__ DF s_gq[NWARP][D2IC_NPART];           // group partials of this block's supergroup
+    __shared__ int s_sgcnt;                          // groups of this block's supergroup reduced this round
     // per warp: two record buffers, then two coefficient-tile buffers (all 128-byte aligned)
     extern __shared__ __align__(128) unsigned char s_dyn[];
     Ctl C = make_ctl(ctl_base, n_frames);
@@ -1030,6 +1038,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     // stamps [3] and [4] around it
     const bool tr = trace != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
     int round = 0;
+    if (threadIdx.x == 0) s_sgcnt = 0;
     // A warp's first chunk of the next round, staged before the round's release (its records,
     // coefficient tile and the metadata of the chunk after it do not depend on the control step);
     // used if the active list is unchanged, else drained.
@@ -1053,7 +1062,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         float4 *ng = reinterpret_cast<float4 *>(F.node_grad);
         for (size_t i = blockIdx.x * NT + threadIdx.x; i < (size_t)F.node_chunk_k * nn; i += (size_t)gridDim.x * NT)
             ng[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        const int n_cnt = F.n_groups + (F.n_groups + GN - 1) / GN + 1;
+        const int n_cnt = F.n_groups + (F.n_groups + SG - 1) / SG + 1;
         for (int i = blockIdx.x * NT + threadIdx.x; i < n_cnt; i += gridDim.x * NT) F.group_cnt[i] = 0;
         if (F.hist)
             for (int i = blockIdx.x * NT + threadIdx.x; i < 3 * F.max_iter; i += gridDim.x * NT)
@@ -1272,7 +1281,10 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             }
             if (trr) trace[7 * round + 1] = gtimer();
             // ---- N work: group gi of the active list goes to global warp gi mod (warps in grid); the
-            // warp waits until every chunk with a node in the group has written its slots ----
+            // warp waits until every chunk with a node in the group has written its slots.  With
+            // at most one group per warp, a supergroup is the warps of one block and is reduced
+            // in shared memory; otherwise through the frame's global partials. ----
+            const bool blockred = tg <= nw;
             int gcur = 0;
             for (int gi = gw; gi < tg; gi += nw) {
                 int s, f, base;
@@ -1288,6 +1300,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 }
                 const d2ic_frame_t &F = frames[f];
                 const int g = gi - base;
+                if (g >= F.n_groups) continue;         // padding of the frame's group range
                 const FInfo fi = cached ? s_fi[s] : frame_info(C.fs + f);
                 const NodePre pre = node_pre(F, fi, g * GN + lane);   // independent of the pixel pass
                 int ok = 1;
@@ -1317,26 +1330,47 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                 node_post(F, fi, g * GN + lane, pre, q);
 #pragma unroll
                 for (int i = 0; i < 5; ++i) q[i] = df_warp_sum(q[i]);
-                // group -> supergroup (32 groups) -> frame: the warp that completes a level reduces it
-                const int ngr = F.n_groups, nsg = (ngr + GN - 1) / GN, sg = g / GN;
+                // group -> supergroup (SG groups) -> frame: the warp that completes a level reduces
+                // it; a supergroup's sum is the same lane-ordered warp sum on both paths
+                const int ngr = F.n_groups, nsg = (ngr + SG - 1) / SG, sg = g / SG;
+                const int members = min(SG, ngr - sg * SG);
                 float2 *gp = reinterpret_cast<float2 *>(F.group_part);
                 int last = 0;
-                if (lane == 0) {
+                if (blockred) {                        // members are warps 0 .. members-1 here
+                    if (lane == 0) {
+#pragma unroll
+                        for (int i = 0; i < 5; ++i) s_gq[wid][i] = q[i];
+                        F.group_cnt[g] = 0;            // every chunk of this round has counted
+                        __threadfence_block();
+                        last = atomicAdd(&s_sgcnt, 1) == members - 1;
+                        if (last) {
+                            s_sgcnt = 0;
+                            __threadfence_block();
+                        }
+                    }
+                } else if (lane == 0) {
 #pragma unroll
                     for (int i = 0; i < 5; ++i) gp[(size_t)g * D2IC_NPART + i] = make_float2(q[i].hi, q[i].lo);
                     F.group_cnt[g] = 0;                // every chunk of this round has counted
-                    const int members = min(GN, ngr - sg * GN);
                     last = atom_acq_rel_add(F.group_cnt + ngr + sg, 1) == members - 1;
                     if (last) F.group_cnt[ngr + sg] = 0;
                 }
                 __syncwarp();
                 if (__shfl_sync(0xffffffffu, last, 0)) {
                     DF v[5];
-                    const int gg = sg * GN + lane;
+                    const int gg = sg * SG + lane;
 #pragma unroll
                     for (int i = 0; i < 5; ++i) {
-                        const float2 t = gg < ngr ? __ldcg(gp + (size_t)gg * D2IC_NPART + i) : make_float2(0.f, 0.f);
-                        v[i] = df_warp_sum(DF{t.x, t.y});
+                        DF t = DF{0.f, 0.f};
+                        if (lane < members) {
+                            if (blockred) {
+                                t = s_gq[lane][i];
+                            } else {
+                                const float2 t2 = __ldcg(gp + (size_t)gg * D2IC_NPART + i);
+                                t = DF{t2.x, t2.y};
+                            }
+                        }
+                        v[i] = df_warp_sum(t);
                     }
                     int lastf = 0;
                     if (lane == 0) {
@@ -1577,7 +1611,7 @@ static size_t ws_layout(int n_nodes, int n_chunks, int node_chunk_k, size_t off[
     off[1] = o;                                               // node_grad
     o += align256(sizeof(float) * 4 * (size_t)node_chunk_k * n_nodes);
     off[2] = o;                                               // group_part
-    const size_t ns = (ng + GN - 1) / GN;                     // supergroups of GN groups
+    const size_t ns = (ng + SG - 1) / SG;                     // supergroups of SG groups
     o += align256(sizeof(float) * 2 * D2IC_NPART * (ng + ns));
     off[3] = o;                                               // group_cnt
     o += align256(sizeof(int) * (ng + ns + 1));
