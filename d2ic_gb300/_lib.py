@@ -66,6 +66,7 @@ _SIGS = {
     "d2ic_frame_descriptor_bytes": (szt, []),
     "d2ic_device_info": (i32, [i32, vp, vp]),
     "d2ic_bspline_prefilter": (i32, [vp, i32, i32, i32, i32, vp, vp, vp]),
+    "d2ic_bspline_prefilter_batch": (i32, [vp, i32, i32, i32, i32, i32, vp, vp, vp]),
     "d2ic_pad_image": (i32, [vp, i32, i32, i32, i32, vp, vp]),
     "d2ic_sample_points": (i32, [vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, vp, vp]),
     "d2ic_pack_pixels": (i32, [vp, vp, i32, vp, i32, i32, i32, i32, i32, vp, vp]),
@@ -82,6 +83,7 @@ _SIGS = {
     "d2ic_hessian_chunks": (i32, [vp, i32, vp, i32, vp, vp]),
     "d2ic_hessian_matvec": (i32, [vp, i32, i32, vp, vp, i32, f32, f32, vp, vp, vp]),
     "d2ic_mixed_term": (i32, [vp, i32, i32, vp, vp, f32, vp, vp, i32, i32, vp]),
+    "d2ic_mixed_term_batch": (i32, [vp, i32, i32, i32, vp, vp, i32, ctypes.c_longlong, f32, vp, vp, i32, i32, vp]),
     "d2ic_mixed_term_T": (i32, [vp, i32, vp, vp, f32, vp, vp]),
     "d2ic_bspline_prefilter_T": (i32, [vp, i32, i32, i32, i32, vp, vp, vp]),
     "d2ic_zncc_match":(i32, [vp, i32, i32, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp]),

@@ -114,16 +114,27 @@ class ImplicitAdjoint:
     def _coeff(self, img: torch.Tensor) -> torch.Tensor:
         return prepare_coefficients(img.to(torch.float32).contiguous(), _lib.INTERP_CUBIC)
 
+    MIXED_BATCH = 32   # images per launch of the batched prefilter and mixed term
+
     def mixed(self, dI: torch.Tensor) -> torch.Tensor:
-        """(d grad_u J / dI2) dI_k for images dI (K, H, W) -> (Nn, 2, K)."""
+        """(d grad_u J / dI2) dI_k for images dI (K, H, W) -> (Nn, 2, K): the images' B-spline
+        coefficients and mixed terms in launches of up to MIXED_BATCH images (the same kernels and
+        arithmetic as one image at a time)."""
         L = self.L
         K = dI.shape[0]
+        H, W = L.H, L.W
         out = torch.empty((L.n_nodes, 2, K), dtype=torch.float32, device=self.dev)
-        slots = torch.zeros(L.node_chunk_k * L.n_nodes * 2, dtype=torch.float32, device=self.dev)
-        for k in range(K):
-            c = self._coeff(dI[k])
-            _lib.call("d2ic_mixed_term", ptr(self.desc), L.n_chunks, L.n_nodes, ptr(self.u), ptr(c), self.inv_np,
-                      ptr(slots), ptr(out), K, k, _lib.stream_handle())
+        B = min(self.MIXED_BATCH, K)
+        slots = torch.zeros(B * L.node_chunk_k * L.n_nodes * 2, dtype=torch.float32, device=self.dev)
+        tmp = torch.empty((B, H, L.cpitch), dtype=torch.float32, device=self.dev)
+        coeff = torch.empty((B, H + 2 * PAD, L.cpitch), dtype=torch.float32, device=self.dev)
+        s = _lib.stream_handle()
+        for k0 in range(0, K, B):
+            nb = min(B, K - k0)
+            imgs = dI[k0:k0 + nb].to(device=self.dev, dtype=torch.float32).contiguous()
+            _lib.call("d2ic_bspline_prefilter_batch", ptr(imgs), nb, H, W, PAD, L.cpitch, ptr(tmp), ptr(coeff), s)
+            _lib.call("d2ic_mixed_term_batch", ptr(self.desc), L.n_chunks, L.n_nodes, L.node_chunk_k, ptr(self.u),
+                      ptr(coeff), nb, (H + 2 * PAD) * L.cpitch, self.inv_np, ptr(slots), ptr(out), K, k0, s)
         return out.to(torch.float64)
 
     def mixed_T(self, lam: torch.Tensor) -> torch.Tensor:

@@ -240,8 +240,11 @@ __global__ void hv_nodes(const d2ic_frame_t *__restrict__ fp, const float *__res
 
 // (d grad_u J / dI2) dI, per chunk into node slots (float2 per node, plane `slot`)
 __global__ void __launch_bounds__(256) mixed_chunks(const d2ic_frame_t *__restrict__ fp, const float2 *__restrict__ u,
-                                                    const float *__restrict__ dcoeff, float2 *__restrict__ slots) {
+                                                    const float *__restrict__ dcoeff, float2 *__restrict__ slots,
+                                                    size_t coeff_stride, size_t slot_stride) {
     const d2ic_frame_t &F = *fp;
+    dcoeff += blockIdx.y * coeff_stride;               // image blockIdx.y of a batch
+    slots += blockIdx.y * slot_stride;
     const int lane = threadIdx.x & 31;
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (c >= F.n_chunks) return;
@@ -284,8 +287,10 @@ __global__ void __launch_bounds__(256) mixed_chunks(const d2ic_frame_t *__restri
 
 // node sum of float2 slots, scaled; writes column k of out (node, comp, K)
 __global__ void slots_to_nodes(const d2ic_frame_t *__restrict__ fp, const float2 *__restrict__ slots, float scale,
-                               float *__restrict__ out, int K, int k) {
+                               float *__restrict__ out, int K, int k0, size_t slot_stride) {
     const d2ic_frame_t &F = *fp;
+    slots += blockIdx.y * slot_stride;                 // image blockIdx.y of a batch -> column k0 + y
+    const int k = k0 + (int)blockIdx.y;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= F.n_nodes) return;
     float sx = 0.f, sy = 0.f;
@@ -412,10 +417,30 @@ extern "C" int d2ic_mixed_term(const d2ic_frame_t *frame_dev, int n_chunks, int 
                  "d2ic_mixed_term: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
     if (n_chunks > 0) {
-        mixed_chunks<<<(n_chunks * 32 + 255) / 256, 256, 0, s>>>(frame_dev, (const float2 *)u, dcoeff, (float2 *)slots);
+        mixed_chunks<<<(n_chunks * 32 + 255) / 256, 256, 0, s>>>(frame_dev, (const float2 *)u, dcoeff, (float2 *)slots,
+                                                                 0, 0);
         D2IC_CHECK_LAUNCH("mixed_chunks");
     }
-    slots_to_nodes<<<(n_nodes + 255) / 256, 256, 0, s>>>(frame_dev, (const float2 *)slots, scale, out, K, k);
+    slots_to_nodes<<<(n_nodes + 255) / 256, 256, 0, s>>>(frame_dev, (const float2 *)slots, scale, out, K, k, 0);
+    D2IC_CHECK_LAUNCH("slots_to_nodes");
+    return D2IC_OK;
+}
+
+extern "C" int d2ic_mixed_term_batch(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
+                                     const float *u, const float *dcoeff, int n_images, long long coeff_stride,
+                                     float scale, float *slots, float *out, int K, int k0, void *stream) {
+    D2IC_REQUIRE(frame_dev && u && dcoeff && slots && out && n_nodes >= 1 && node_chunk_k >= 1 && n_images >= 1 &&
+                     n_images < 65536 && k0 >= 0 && k0 + n_images <= K && coeff_stride > 0,
+                 "d2ic_mixed_term_batch: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t slot_stride = (size_t)node_chunk_k * n_nodes;   // float2 per image
+    if (n_chunks > 0) {
+        mixed_chunks<<<dim3((n_chunks * 32 + 255) / 256, n_images), 256, 0, s>>>(
+            frame_dev, (const float2 *)u, dcoeff, (float2 *)slots, (size_t)coeff_stride, slot_stride);
+        D2IC_CHECK_LAUNCH("mixed_chunks");
+    }
+    slots_to_nodes<<<dim3((n_nodes + 255) / 256, n_images), 256, 0, s>>>(frame_dev, (const float2 *)slots, scale, out,
+                                                                         K, k0, slot_stride);
     D2IC_CHECK_LAUNCH("slots_to_nodes");
     return D2IC_OK;
 }

@@ -33,10 +33,13 @@ static int ensure_fir() {
     return D2IC_OK;
 }
 
-// rows: tmp[y][cx] = sum_k h[k] img[y][clamp(cx - pad + k)], cx in [0, W + 2 pad)
+// rows: tmp[y][cx] = sum_k h[k] img[y][clamp(cx - pad + k)], cx in [0, W + 2 pad); image
+// blockIdx.z of a batch (contiguous images and buffers)
 __global__ void __launch_bounds__(256) prefilter_rows(const float *__restrict__ img, int H, int W, int pad,
                                                       int cpitch, float *__restrict__ tmp) {
     __shared__ float s[256 + 2 * KF];
+    img += (size_t)blockIdx.z * H * W;
+    tmp += (size_t)blockIdx.z * H * cpitch;
     const int y = blockIdx.y;
     const int cx0 = blockIdx.x * 256;
     const float *row = img + (size_t)y * W;
@@ -59,6 +62,8 @@ constexpr int CT_W = 32, CT_H = 64;
 __global__ void __launch_bounds__(256) prefilter_cols(const float *__restrict__ tmp, int H, int W, int pad,
                                                       int cpitch, float *__restrict__ coeff) {
     __shared__ float s[CT_H + 2 * KF][CT_W + 1];
+    tmp += (size_t)blockIdx.z * H * cpitch;
+    coeff += (size_t)blockIdx.z * (H + 2 * pad) * cpitch;
     const int cx = blockIdx.x * CT_W + threadIdx.x;
     const int cy0 = blockIdx.y * CT_H;
     const int CW = W + 2 * pad;
@@ -117,6 +122,25 @@ __global__ void pack_pixels_kernel(const int2 *__restrict__ colrow, const float2
 }  // namespace d2ic
 
 using namespace d2ic;
+
+extern "C" int d2ic_bspline_prefilter_batch(const float *img, int n_images, int H, int W, int pad, int cpitch,
+                                            float *tmp, float *coeff, void *stream) {
+    D2IC_REQUIRE(img && tmp && coeff, "d2ic_bspline_prefilter_batch: null pointer");
+    D2IC_REQUIRE(n_images >= 1 && n_images < 65536, "d2ic_bspline_prefilter_batch: bad image count %d", n_images);
+    D2IC_REQUIRE(H > 0 && W > 0 && H < 65536 && W < 65536, "d2ic_bspline_prefilter_batch: bad image size %dx%d", H, W);
+    D2IC_REQUIRE(pad >= KF && cpitch >= W + 2 * pad,
+                 "d2ic_bspline_prefilter_batch: need pad >= %d and cpitch >= W + 2 pad", KF);
+    int st = ensure_fir();
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int CW = W + 2 * pad;
+    prefilter_rows<<<dim3((CW + 255) / 256, H, n_images), 256, 0, s>>>(img, H, W, pad, cpitch, tmp);
+    D2IC_CHECK_LAUNCH("prefilter_rows");
+    prefilter_cols<<<dim3((CW + CT_W - 1) / CT_W, (H + 2 * pad + CT_H - 1) / CT_H, n_images), dim3(CT_W, 8), 0, s>>>(
+        tmp, H, W, pad, cpitch, coeff);
+    D2IC_CHECK_LAUNCH("prefilter_cols");
+    return D2IC_OK;
+}
 
 extern "C" int d2ic_bspline_prefilter(const float *img, int H, int W, int pad, int cpitch, float *tmp,
                                       float *coeff, void *stream) {

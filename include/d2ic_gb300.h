@@ -132,6 +132,10 @@ D2IC_API int d2ic_device_info(int device, int *num_sms, int *engine_blocks_per_s
  * tmp: H x cpitch floats of scratch.  pad >= 16, cpitch >= W + 2 pad. */
 D2IC_API int d2ic_bspline_prefilter(const float *img, int H, int W, int pad, int cpitch,
                            float *tmp, float *coeff, void *stream);
+/* The same for n_images contiguous HxW images in one launch: image i's scratch at
+ * tmp + i H cpitch and its coefficients at coeff + i (H + 2 pad) cpitch. */
+D2IC_API int d2ic_bspline_prefilter_batch(const float *img, int n_images, int H, int W, int pad, int cpitch,
+                                          float *tmp, float *coeff, void *stream);
 
 /* Copy an image into the halo layout with edge replication (linear kind). */
 D2IC_API int d2ic_pad_image(const float *img, int H, int W, int pad, int cpitch, float *out, void *stream);
@@ -313,6 +317,12 @@ D2IC_API int d2ic_hessian_matvec(const d2ic_frame_t *frame_dev, int n_chunks, in
  * B-spline coefficients (halo layout of the frame).  slots: node_chunk_k * n_nodes * 2 floats. */
 D2IC_API int d2ic_mixed_term(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, const float *u,
                              const float *dcoeff, float scale, float *slots, float *out, int K, int k, void *stream);
+/* The same for n_images coefficient images in one launch (image i at dcoeff + i coeff_stride
+ * floats) into columns k0 .. k0 + n_images - 1; slots: n_images * node_chunk_k * n_nodes * 2
+ * floats, zero where no chunk writes (zeroed once by the caller). */
+D2IC_API int d2ic_mixed_term_batch(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
+                                   const float *u, const float *dcoeff, int n_images, long long coeff_stride,
+                                   float scale, float *slots, float *out, int K, int k0, void *stream);
 /* Adjoint of d2ic_mixed_term: gcoeff (halo layout, zeroed by the caller) += scale *
  * (d grad_u J / dI2 coefficients)^T lambda, by atomic scatter (backward of the bicubic sampling). */
 D2IC_API int d2ic_mixed_term_T(const d2ic_frame_t *frame_dev, int n_chunks, const float *u, const float *lam,
