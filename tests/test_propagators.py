@@ -62,3 +62,50 @@ def test_batch_uses_the_propagator_for_warm_starts():
     b.sequence(frames)
     assert prop.calls == [(None, None), (1.0, None), (2.0, 1.0), (3.0, 2.0)]
     assert dic.guesses == [1.0, 3.0, 4.0]                      # 2*1-1, 2*2-1, 2*3-2
+
+
+def test_overlapped_loop_order_and_warm_starts():
+    """The overlapped sequence loop (run on the host here with a stand-in DIC): frame k + 1 is
+    queued before frame k is collected, the warm start of frame k + 1 is the constant-velocity
+    extrapolation of the two previous solutions, and results come back in frame order."""
+    import torch
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300.batch_mesh_based import BatchMeshBased
+    from d2ic_gb300.dataclasses import BatchConfig, DICDiagnostics, DICResult
+
+    events = []
+
+    class Pending:
+        def __init__(self, k, u):
+            self.k, self.u_device = k, u
+
+    class FakeDIC:
+        def __init__(self):
+            self.k, self.guess = 0, None
+
+        def prepare(self, ref, assets):
+            pass
+
+        def set_initial_guess(self, u):
+            self.guess = u
+
+        def run_begin(self, img):
+            self.k += 1
+            events.append(("begin", self.k, None if self.guess is None else float(self.guess[0, 0])))
+            return Pending(self.k, torch.full((3, 2), float(self.k * self.k)))
+
+        def run_end(self, p):
+            events.append(("end", p.k))
+            return DICResult(u_nodal=p.u_device.numpy().copy(), strain=np.zeros((3, 3)),
+                             diagnostics=DICDiagnostics(info={"frame": p.k}))
+
+    dic = FakeDIC()
+    b = BatchMeshBased(np.zeros((4, 4), np.float32), None, dic, BatchConfig(),
+                       propagator=d2.ConstantVelocityPropagator())
+    per_frame, lat = [], []
+    b._sequence_pipelined([np.zeros((4, 4), np.float32)] * 4, per_frame, lat, False, None, False, 4)
+    # solutions k^2: warm starts none, 1 (previous only), 2*4-1 = 7, 2*9-4 = 14
+    assert events == [("begin", 1, None), ("begin", 2, 1.0), ("end", 1), ("begin", 3, 7.0), ("end", 2),
+                      ("begin", 4, 14.0), ("end", 3), ("end", 4)]
+    assert [r.diagnostics.info["frame"] for r in per_frame] == [1, 2, 3, 4] and len(lat) == 4
