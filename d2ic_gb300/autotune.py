@@ -47,7 +47,8 @@ def frame_signature(pix, H: int, W: int, interpolation: str) -> str:
     elem = 0
     if n_pix:
         # the most common pixels-per-element count (interior elements), as an element-size estimate
-        counts = np.bincount(np.unique(_elements_of(pix), return_counts=True)[1])
+        per_elem = np.bincount(_elements_of(pix))
+        counts = np.bincount(per_elem[per_elem > 0])
         elem = int(round(np.sqrt(int(np.argmax(counts)))))
     bucket = int(round(64 * np.log2(max(n_pix, 1))))
     return f"{H}x{W}:{interpolation}:e{elem}:p{bucket}"

@@ -22,19 +22,40 @@ from __future__ import annotations
 
 import numpy as np
 
-from .mesh_assets import Mesh, PixelAssets
+from .mesh_assets import Mesh, PixelAssets, unique_sorted
 
 _TOL = 1e-6
 
 
-def _sample_pixels_in_bbox(nodes: np.ndarray, H: int, W: int, pad: float) -> np.ndarray:
-    """Pixel centres ``(j+0.5, i+0.5)`` of the padded node bbox, rows outer (d2ic/pixel_assets.py:115-132)."""
+def _bbox(nodes: np.ndarray, H: int, W: int, pad: float):
+    """Pixel rows [i0, i1) and columns [j0, j1) of the padded node bbox, inside the image."""
     j0 = max(0, int(np.floor(nodes[:, 0].min() - pad)))
     j1 = min(W, int(np.ceil(nodes[:, 0].max() + pad)))
     i0 = max(0, int(np.floor(nodes[:, 1].min() - pad)))
     i1 = min(H, int(np.ceil(nodes[:, 1].max() + pad)))
+    return i0, i1, j0, j1
+
+
+def _sample_pixels_in_bbox(nodes: np.ndarray, H: int, W: int, pad: float) -> np.ndarray:
+    """Pixel centres ``(j+0.5, i+0.5)`` of the padded node bbox, rows outer (d2ic/pixel_assets.py:115-132)."""
+    i0, i1, j0, j1 = _bbox(nodes, H, W, pad)
     jj, ii = np.meshgrid(np.arange(j0, j1), np.arange(i0, i1))
     return np.stack([jj.ravel() + 0.5, ii.ravel() + 0.5], axis=1)
+
+
+def _roi_pixels(nodes: np.ndarray, H: int, W: int, pad: float, roi_mask):
+    """The bbox pixels kept by the ROI mask (all of them without one), rows outer, as integer
+    rows and columns: the same pixels and order as sampling the bbox and then testing the mask at
+    ``floor(centre - 0.5)`` (d2ic/pixel_assets.py:115-132), without forming the whole bbox."""
+    i0, i1, j0, j1 = _bbox(nodes, H, W, pad)
+    if i1 <= i0 or j1 <= j0:
+        z = np.zeros((0,), dtype=np.int64)
+        return z, z
+    if roi_mask is None:
+        ii, jj = np.divmod(np.arange((i1 - i0) * (j1 - j0), dtype=np.int64), j1 - j0)
+    else:
+        ii, jj = np.nonzero(roi_mask[i0:i1, j0:j1])
+    return ii.astype(np.int64) + i0, jj.astype(np.int64) + j0
 
 
 def structured_grid(nodes: np.ndarray, elements: np.ndarray):
@@ -178,16 +199,15 @@ def structured_assign_device(pc: np.ndarray, gx, gy, cell, device=None) -> np.nd
     return out.cpu().numpy()
 
 
-def _pixel_elements(pc: np.ndarray, nodes: np.ndarray, el: np.ndarray):
-    """``build_pixel_to_element_mapping_numpy`` with the tensor-grid search on the GPU when one
-    is present (identical results)."""
-    if pc.shape[0] > 0 and el.size > 0 and _gpu_available():
-        sg = structured_grid(nodes, el)
-        if sg is not None:
-            elts = structured_assign_device(pc, *sg)
-            pn = np.where((elts >= 0)[:, None], el[np.maximum(elts, 0)], 0)
-            return elts, pn
-    return build_pixel_to_element_mapping_numpy(pc, nodes, el)
+def _pixel_element_ids(pc: np.ndarray, nodes: np.ndarray, el: np.ndarray) -> np.ndarray:
+    """The element of each pixel (-1 outside), as ``build_pixel_to_element_mapping_numpy``, with
+    the tensor-grid search on the GPU when one is present (identical results)."""
+    if pc.shape[0] == 0 or el.size == 0:
+        return -np.ones((pc.shape[0],), dtype=np.int64)
+    sg = structured_grid(nodes, el)
+    if sg is not None:
+        return structured_assign_device(pc, *sg) if _gpu_available() else _structured_assign(pc, *sg)
+    return _generic_assign(pc, nodes, el)
 
 
 def _solve2(a11, a12, a21, a22, b1, b2):
@@ -253,8 +273,18 @@ def local_coordinates(pixel_coords, pixel_nodes, nodes_coord, iters: int = 10):
 
 def shape_functions(xi, eta) -> np.ndarray:
     """Q4 shape functions, node order (-1,-1), (1,-1), (1,1), (-1,1)."""
-    return np.stack([0.25 * (1 - xi) * (1 - eta), 0.25 * (1 + xi) * (1 - eta),
-                     0.25 * (1 + xi) * (1 + eta), 0.25 * (1 - xi) * (1 + eta)], axis=-1)
+    xi, eta = np.asarray(xi), np.asarray(eta)
+    if xi.ndim != 1 or eta.ndim != 1:
+        return np.stack([0.25 * (1 - xi) * (1 - eta), 0.25 * (1 + xi) * (1 - eta),
+                         0.25 * (1 + xi) * (1 + eta), 0.25 * (1 - xi) * (1 + eta)], axis=-1)
+    a0, a1 = 0.25 * (1 - xi), 0.25 * (1 + xi)       # the same products, left to right
+    b0, b1 = 1 - eta, 1 + eta
+    N = np.empty((xi.shape[0], 4), dtype=np.result_type(a0, b0))
+    np.multiply(a0, b0, out=N[:, 0])
+    np.multiply(a1, b0, out=N[:, 1])
+    np.multiply(a1, b1, out=N[:, 2])
+    np.multiply(a0, b1, out=N[:, 3])
+    return N
 
 
 def local_coordinates_device(pixel_coords, pixel_nodes, nodes_coord, iters: int = 10, device=None):
@@ -315,7 +345,7 @@ def build_node_neighbor_dense(elements, nodes_coord, n_nodes):
     m = (a != b).ravel()
     src = el[:, a.ravel()[m]].ravel()
     dst = el[:, b.ravel()[m]].ravel()
-    key = np.unique(src * n_nodes + dst)            # unique pairs, ordered by (src, dst)
+    key = unique_sorted(src * n_nodes + dst)        # unique pairs, ordered by (src, dst)
     src, dst = key // n_nodes, key % n_nodes
     deg = np.bincount(src, minlength=n_nodes).astype(np.int32)
     maxd = int(deg.max(initial=0))
@@ -363,20 +393,18 @@ def build_pixel_assets(mesh: Mesh, ref_image, binning: float, roi_mask=None, bbo
         roi_mask = np.asarray(roi_mask, dtype=bool)
         if roi_mask.shape != (H, W):
             raise ValueError(f"roi_mask shape {roi_mask.shape} does not match ref_image shape {(H, W)}")
-    pc = _sample_pixels_in_bbox(nodes, H, W, bbox_pad)
-    if roi_mask is not None and pc.size > 0:
-        rows = np.clip(np.floor(pc[:, 1] - 0.5).astype(int), 0, H - 1)
-        cols = np.clip(np.floor(pc[:, 0] - 0.5).astype(int), 0, W - 1)
-        pc = pc[roi_mask[rows, cols]]
     if chunk_size < 1:
         raise ValueError("chunk_size must be >= 1")
-    elts, pn = _pixel_elements(pc, nodes, elements)
+    rows, cols = _roi_pixels(nodes, H, W, bbox_pad, roi_mask)
+    pc = np.empty((rows.size, 2), dtype=np.float64)
+    pc[:, 0] = cols + 0.5
+    pc[:, 1] = rows + 0.5
+    elts = _pixel_element_ids(pc, nodes, elements)
     keep = elts >= 0
-    pc, pn, elts = pc[keep], pn[keep], elts[keep]
+    pc, elts, rows, cols = pc[keep], elts[keep], rows[keep], cols[keep]
+    pn = elements[elts]
     N, xe = compute_pixel_shape_functions(pc, pn, nodes)
     nidx, ndeg, nw = build_node_neighbor_dense(elements, nodes, nodes.shape[0])
-    rows = np.clip(np.floor(pc[:, 1] - 0.5).astype(int), 0, H - 1)
-    cols = np.clip(np.floor(pc[:, 0] - 0.5).astype(int), 0, W - 1)
     return PixelAssets(
         pixel_coords_ref=pc, pixel_nodes=pn.astype(np.int32), pixel_shapeN=N,
         node_neighbor_index=nidx, node_neighbor_degree=ndeg, node_neighbor_weight=nw,

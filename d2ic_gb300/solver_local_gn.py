@@ -80,7 +80,7 @@ class LocalGaussNewtonSolver(SolverBase):
         self._nbw = T(np.where(valid, w, 0).astype(np.float32).T.copy(), torch.float32) if md else None
         self._rho = T(np.asarray(pix.node_reg_weight, dtype=np.float32), torch.float32)
         has = np.zeros(nn, dtype=np.int32)
-        has[np.unique(np.asarray(pix.pixel_nodes))] = 1
+        has[np.asarray(pix.pixel_nodes).ravel()] = 1
         self._has_pix = T(has, torch.int32)
         self._slots = torch.zeros(_lib.load().d2ic_local_gn_slot_bytes(nn, L.node_chunk_k) // 4, dtype=torch.float32,
                                   device=dev)
