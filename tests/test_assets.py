@@ -70,3 +70,28 @@ def test_build_errors_match_reference():
         d2.mask_to_mesh(np.zeros((20, 20), bool), 8)
     with pytest.raises(ValueError):
         d2.mask_to_mesh(np.ones((20, 20), bool), 0)
+
+
+def test_host_helpers_match_numpy_forms():
+    """The host fast paths give exactly what the plain numpy forms give: sort-based unique of
+    edge keys, shape functions without the stacking copy, ROI pixels from the mask window."""
+    from d2ic_gb300.mesh_assets import unique_sorted
+    from d2ic_gb300.pixel_assets import _roi_pixels, _sample_pixels_in_bbox, shape_functions
+    rng = np.random.default_rng(7)
+    keys = rng.integers(0, 10 ** 9, 100000)
+    assert np.array_equal(unique_sorted(keys), np.unique(keys)) and unique_sorted(keys[:0]).size == 0
+    xi, eta = rng.uniform(-1, 1, 1000), rng.uniform(-1, 1, 1000)
+    ref = np.stack([0.25 * (1 - xi) * (1 - eta), 0.25 * (1 + xi) * (1 - eta),
+                    0.25 * (1 + xi) * (1 + eta), 0.25 * (1 - xi) * (1 + eta)], axis=-1)
+    assert np.array_equal(shape_functions(xi, eta), ref)
+    H, W = 61, 47
+    nodes = np.array([[3.2, 4.9], [40.1, 4.9], [40.1, 55.3], [3.2, 55.3]])
+    roi = rng.random((H, W)) > 0.3
+    for mask in (roi, None):
+        pc = _sample_pixels_in_bbox(nodes, H, W, 2.0)
+        if mask is not None:
+            rows = np.clip(np.floor(pc[:, 1] - 0.5).astype(int), 0, H - 1)
+            cols = np.clip(np.floor(pc[:, 0] - 0.5).astype(int), 0, W - 1)
+            pc = pc[mask[rows, cols]]
+        r, c = _roi_pixels(nodes, H, W, 2.0, mask)
+        assert np.array_equal(np.stack([c + 0.5, r + 0.5], axis=1), pc)
