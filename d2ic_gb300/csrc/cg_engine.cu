@@ -17,7 +17,7 @@
 //                spring gradient over the neighbour table, writes the trial
 //                gradient, point and direction, and reduces (fixed order) sum
 //                r^2, spring energy, g.g, g.(g - g_cur), g_cur.dir; the warp
-//                that completes a supergroup of 32 groups reduces it, and the
+//                that completes a supergroup of 16 groups reduces it, and the
 //                warp that completes a frame's last supergroup runs the CG
 //                control of d2ic/solver_global_cg.py:362-461 (stop test, PR+
 //                beta, restart on g.d >= 0, Armijo with 10 halvings and the
@@ -39,6 +39,8 @@
 #include <cuda.h>   // CUtensorMap and its enums (the encoder is fetched from the driver at run time)
 #include <stddef.h>
 #include <string.h>
+
+#include <atomic>
 
 #include "common.cuh"
 
@@ -1601,8 +1603,8 @@ extern "C" size_t d2ic_cg_control_bytes(int n_frames) {
 // Workspace of one frame: 7 node buffers (u x2, g x3, dir x2), the K gradient
 // slots per node (16 bytes: gx, gy and the chunk's r^2 sum as a double-float),
 // the partials (D2IC_NPART double-float pairs) of every group and then of every
-// supergroup of 32 groups, the completion counters (groups, supergroups, the
-// frame's count of supergroups), and the tile origins.
+// supergroup of SG groups, the completion counters (groups, supergroups, the
+// frame's count of supergroups), and the tile origins (4 bytes per chunk).
 static size_t ws_layout(int n_nodes, int n_chunks, int node_chunk_k, size_t off[5]) {
     const size_t ng = (size_t)(n_nodes + GN - 1) / GN;
     size_t o = 0;
@@ -1756,7 +1758,18 @@ extern "C" int d2ic_eval_objective(const d2ic_frame_t *frame, const float *u, vo
 // array instead of caller memory.  Every GPU that loads the library holds the
 // array until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[D2IC_NOALLOC_SCRATCH_BYTES];
-static void *g_noalloc_addr[64];   // device address of the array, per device (host-side stand-in is not usable)
+// device address of the array, per device (the host-side name is a stand-in, not a device address);
+// atomic so that threads making their first call on a device at the same time do not race
+static std::atomic<void *> g_noalloc_addr[64];
+
+// Writes a frame descriptor into the scratch array.  The descriptor travels as a kernel argument,
+// copied at launch, so no host buffer has to outlive the call and the host does not wait.
+__global__ void noalloc_put_descriptor(const d2ic_frame_t f, d2ic_frame_t *dst) {
+    static_assert(sizeof(d2ic_frame_t) % 8 == 0, "descriptor copied in 8-byte words");
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&f);
+    unsigned long long *d = reinterpret_cast<unsigned long long *>(dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(d2ic_frame_t) / 8); i += blockDim.x) d[i] = src[i];
+}
 
 extern "C" int d2ic_cg_solve_noalloc(const d2ic_frame_t *frame, int interp_kind, void *stream) {
     D2IC_REQUIRE(frame, "d2ic_cg_solve_noalloc: null frame");
@@ -1774,20 +1787,19 @@ extern "C" int d2ic_cg_solve_noalloc(const d2ic_frame_t *frame, int interp_kind,
                  "d2ic_cg_solve_noalloc: frame needs %zu bytes of scratch (%d nodes, %d chunks), more than the "
                  "fixed %zu-byte array; use d2ic_cg_solve_batched with caller-allocated scratch",
                  need, frame->n_nodes, frame->n_chunks, (size_t)D2IC_NOALLOC_SCRATCH_BYTES);
-    if (g_noalloc_addr[dev] == nullptr) {      // set-up, once per device, with that device current
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    void *addr = g_noalloc_addr[dev].load(std::memory_order_relaxed);
+    if (addr == nullptr) {                     // set-up, once per device, with that device current
+        e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(noalloc scratch)");
-        g_noalloc_addr[dev] = p;
+        g_noalloc_addr[dev].store(addr, std::memory_order_relaxed);
     }
-    char *base = (char *)g_noalloc_addr[dev];
+    char *base = (char *)addr;
     d2ic_frame_t f = *frame;                   // caller's inputs/outputs, workspace from the array
     int st = d2ic_frame_bind_workspace(&f, base + desc_bytes + ctl_bytes);
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
-    // pageable-source copy: returns once `f` has been staged, so the stack copy may go out of scope
-    e = cudaMemcpyAsync(base, &f, sizeof(f), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return cuda_status(e, "noalloc descriptor copy");
+    noalloc_put_descriptor<<<1, 64, 0, s>>>(f, (d2ic_frame_t *)base);
+    D2IC_CHECK_LAUNCH("noalloc descriptor write");
     // the launch clears the control header on `s`; the kernel initialises every workspace word it reads
     return launch_engine((const d2ic_frame_t *)base, 1, base + desc_bytes, ctl_bytes, interp_kind, 0, 0, nullptr,
                          nullptr, nullptr, nullptr, 0, s);

@@ -99,7 +99,7 @@ typedef struct d2ic_frame {
                                       (slot k of node n at k * n_nodes + n), unused slots 0 */
     float       *group_part;       /* 2 * D2IC_NPART * (n_groups + n_super) double-float
                                       partials of the groups, then of the supergroups of
-                                      32 groups (n_super = ceil(n_groups / 32))          */
+                                      16 groups (n_super = ceil(n_groups / 16))          */
     int         *group_cnt;        /* n_groups + n_super + 1 completion counters (all 0
                                       between rounds)                                   */
     int         *chunk_tile;       /* n_chunks: origin (col | row << 16, int16 each) of the
@@ -139,6 +139,7 @@ D2IC_API int d2ic_bspline_prefilter_batch(const float *img, int n_images, int H,
 
 /* Copy an image into the halo layout with edge replication (linear kind). */
 D2IC_API int d2ic_pad_image(const float *img, int H, int W, int pad, int cpitch, float *out, void *stream);
+
 
 /* Sample n points at image-index coordinates xy (x = col, y = row, i.e. the
  * reference's pixel-centre coordinates minus 0.5); value and d/dx, d/dy.
@@ -267,6 +268,7 @@ D2IC_API size_t d2ic_cg_command_offset(void);
 D2IC_API int d2ic_cg_slice(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
                            int interp_kind, int grid_blocks, int max_rounds, void *stream);
 
+
 /* As d2ic_cg_solve_batched, and writes 6 %globaltimer stamps per round into
  * trace[6*r .. 6*r+5] for r < trace_rounds: block 0's round start, end of the
  * pixel-pass barrier and end of its node pass; start and end of the control
@@ -283,8 +285,10 @@ D2IC_API int d2ic_cg_solve_traced(const d2ic_frame_t *frames, int n_frames, void
  * descriptor copy, control block and CG workspace come from one fixed
  * file-scope device array of D2IC_NOALLOC_SCRATCH_BYTES, which every GPU that
  * loads the library holds until the process exits.  A frame needing more
- * (about (56 + 8 node_chunk_k) B per node + 8 B per chunk + 2 KB) is rejected
- * with D2IC_BAD_ARG.
+ * (about (57.5 + 16 node_chunk_k) B per node + 4 B per chunk + under 4 KB of
+ * descriptor, control block and alignment) is rejected with D2IC_BAD_ARG.
+ * The descriptor is written into the array by a small kernel that receives it
+ * as a launch argument, so `frame` may be reused or freed when the call returns.
  * The first call on a device looks up the array's device address (set-up), so
  * make it before any stream capture.  All calls share the one array and the
  * last call's contents stay in it: calls whose work overlaps on the GPU race.

@@ -7,7 +7,9 @@ one solve entry point whose scratch (descriptor copy, control block, CG
 workspace) lives in a fixed-size device array inside the library.  This test
 calls it through the C ABI twice in a row and checks each result against the
 regular, caller-allocated entry point (d2ic_cg_solve_batched) on the same
-inputs, within the nodal tolerance used by the other parity tests (1e-3 px).
+inputs, within the nodal tolerance used by the other parity tests (1e-3 px),
+then once more on a smaller frame, so that counters and tile origins left in
+the shared array by a larger frame cannot leak into a smaller one.
 It is collected last so that a failure here cannot hide another test's.
 """
 from __future__ import annotations
@@ -22,13 +24,13 @@ pytestmark = pytest.mark.gpu
 TOL_PX = 1e-3
 
 
-def _frame(device):
+def _frame(device, side=256, roi=224, seed=11):
     import d2ic_gb300 as d2
     from d2ic_gb300 import engine
     from d2ic_gb300.synthetic import Translation, rect_mask, speckle_sequence
-    H = W = 256
-    ref, frames = speckle_sequence(H, W, [Translation(0.8, -0.45)], seed=11, noise_seeds=[11, 12])
-    mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, W, 224, 224), 16)
+    H = W = side
+    ref, frames = speckle_sequence(H, W, [Translation(0.8, -0.45)], seed=seed, noise_seeds=[seed, seed + 1])
+    mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, W, roi, roi), 16)
     pix = d2.build_pixel_assets(mesh, ref, 1.0, assets.roi_mask)
     layout = engine.FrameLayout(pix, mesh.nodes_xy.shape[0], ref, "cubic", device)
     slot = engine.FrameSlot(layout, max_iter=120)
@@ -38,19 +40,27 @@ def _frame(device):
     return layout, slot
 
 
-def test_noalloc_matches_regular_entry_point_twice(cuda):
-    from d2ic_gb300 import _lib, engine
-    layout, slot = _frame(cuda)
-    # regular entry point, caller-allocated scratch
+def _regular(cuda, layout, slot):
+    """The regular entry point (d2ic_cg_solve_batched, caller-allocated scratch)."""
+    from d2ic_gb300 import engine
     eng = engine.Engine(cuda, 1)
     eng.solve(engine.descriptors_to_device([slot.desc], cuda), 1, layout.kind)
     torch.cuda.synchronize()
-    u_ref = slot.u_out.clone()
-    info_ref = slot.info.clone()
-    assert int(info_ref[0]) > 5
-    # allocation-free entry point: same inputs, separate outputs, host descriptor
-    desc = _lib.Frame.from_buffer_copy(bytes(slot.desc))
-    for call in range(2):
+    return slot.u_out.clone(), slot.info.clone()
+
+
+def test_noalloc_matches_regular_entry_point_on_consecutive_calls(cuda):
+    from d2ic_gb300 import _lib
+    big = _frame(cuda)
+    small = _frame(cuda, side=128, roi=96, seed=13)
+    refs = [_regular(cuda, *big), _regular(cuda, *small)]
+    assert int(refs[0][1][0]) > 5 and int(refs[1][1][0]) > 5
+    # allocation-free entry point: same inputs, separate outputs, host descriptor; two calls on
+    # the 256 x 256 frame, then one on the 128 x 128 frame
+    for call, which in enumerate((0, 0, 1)):
+        layout, slot = (big, small)[which]
+        u_ref, info_ref = refs[which]
+        desc = _lib.Frame.from_buffer_copy(bytes(slot.desc))
         u_out = torch.full_like(slot.u_out, float("nan"))
         hist = torch.full_like(slot.hist, float("nan"))
         info = torch.zeros(3, dtype=torch.int32, device=cuda)
@@ -61,6 +71,8 @@ def test_noalloc_matches_regular_entry_point_twice(cuda):
         desc.n_evals = info.data_ptr() + 8
         rc = _lib.load().d2ic_cg_solve_noalloc(ctypes.byref(desc), layout.kind, _lib.stream_handle())
         assert rc == 0, _lib.load().d2ic_last_error_string()
+        # the descriptor went to the device with the launch: the host copy may be reused at once
+        ctypes.memset(ctypes.addressof(desc), 0, ctypes.sizeof(desc))
         torch.cuda.synchronize()
         err = float((u_out - u_ref).abs().max())
         assert err <= TOL_PX, f"call {call}: max nodal difference {err:.3e} px"
