@@ -37,6 +37,10 @@ def lib():
         L.oracle_pixel_terms.argtypes = [dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ip, dp, dp,
                                          ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, dp, dp, ctypes.c_int]
         L.oracle_pixel_terms.restype = None
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.oracle_pixel_terms_f32.argtypes = [fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ip, fp, fp,
+                                             ctypes.c_int, fp, ctypes.c_int, ctypes.c_float, dp, fp, ctypes.c_int]
+        L.oracle_pixel_terms_f32.restype = None
         _LIB = L
     return _LIB
 
@@ -46,31 +50,50 @@ def _p(a, t=ctypes.c_double):
 
 
 class FastProblem:
-    """Cubic-interpolation objective on a :class:`Problem`, pixel term in C."""
+    """Cubic-interpolation objective on a :class:`Problem`, pixel term in C.
 
-    def __init__(self, pb: Problem, nthreads: int | None = None):
+    ``precision="f64"`` is the oracle.  ``precision="f32"`` runs the same pixel
+    arithmetic in float32 (the reference's default x32 precision) and serves
+    only as an x32-equivalent CPU timing; the CG control stays in FP64 numpy.
+    """
+
+    def __init__(self, pb: Problem, nthreads: int | None = None, precision: str = "f64"):
         assert pb.interpolation == "cubic"
+        assert precision in ("f64", "f32")
         self.pb = pb
+        self.precision = precision
+        dt = np.float64 if precision == "f64" else np.float32
+        self.dt = dt
         self.nthreads = nthreads or os.cpu_count() or 1
-        self.coeff2 = np.ascontiguousarray(pb.coeff2, dtype=np.float64)
-        self.coords = np.ascontiguousarray(pb.pixel_coords, dtype=np.float64)
+        self.coeff2 = np.ascontiguousarray(pb.coeff2, dtype=dt)
+        self.coords = np.ascontiguousarray(pb.pixel_coords, dtype=dt)
         self.pnodes = np.ascontiguousarray(pb.pixel_nodes, dtype=np.int32)
-        self.N = np.ascontiguousarray(pb.pixel_shapeN, dtype=np.float64)
+        self.N = np.ascontiguousarray(pb.pixel_shapeN, dtype=dt)
         self.I1 = np.ascontiguousarray(
-            cubic_sample(pb.coeff1, ORACLE_PAD, pb.pixel_coords[:, 0] - 0.5, pb.pixel_coords[:, 1] - 0.5))
+            cubic_sample(pb.coeff1, ORACLE_PAD, pb.pixel_coords[:, 0] - 0.5, pb.pixel_coords[:, 1] - 0.5), dtype=dt)
         self.Np = self.coords.shape[0]
 
     def _pixel(self, u, want_grad):
-        u = np.ascontiguousarray(u, dtype=np.float64)
+        dt = self.dt
+        u = np.ascontiguousarray(u, dtype=dt)
         Nn = u.shape[0]
         s = ctypes.c_double(0.0)
         denom = max(self.Np, 1)
-        g = np.zeros((Nn, 2)) if want_grad else None
+        g = np.zeros((Nn, 2), dtype=dt) if want_grad else None
         Hc, Wc = self.coeff2.shape
-        lib().oracle_pixel_terms(_p(self.coeff2), Hc, Wc, ORACLE_PAD, _p(self.coords),
-                                 _p(self.pnodes, ctypes.c_int), _p(self.N), _p(self.I1), self.Np,
-                                 _p(u), Nn, 1.0 / denom, ctypes.byref(s),
-                                 _p(g) if want_grad else None, self.nthreads)
+        if self.precision == "f64":
+            lib().oracle_pixel_terms(_p(self.coeff2), Hc, Wc, ORACLE_PAD, _p(self.coords),
+                                     _p(self.pnodes, ctypes.c_int), _p(self.N), _p(self.I1), self.Np,
+                                     _p(u), Nn, 1.0 / denom, ctypes.byref(s),
+                                     _p(g) if want_grad else None, self.nthreads)
+        else:
+            f = ctypes.c_float
+            lib().oracle_pixel_terms_f32(_p(self.coeff2, f), Hc, Wc, ORACLE_PAD, _p(self.coords, f),
+                                         _p(self.pnodes, ctypes.c_int), _p(self.N, f), _p(self.I1, f), self.Np,
+                                         _p(u, f), Nn, 1.0 / denom, ctypes.byref(s),
+                                         _p(g, f) if want_grad else None, self.nthreads)
+            if g is not None:
+                g = g.astype(np.float64)
         return 0.5 * s.value / denom, g
 
     def value(self, u, alpha_reg):

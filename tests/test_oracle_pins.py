@@ -140,6 +140,18 @@ def test_c_pixel_term_matches_numpy():
     assert np.abs(g1 - g2).max() <= 1e-12 * np.abs(g1).max()
 
 
+def test_c_pixel_term_f32_is_the_same_objective_in_float32():
+    """The x32-equivalent timing variant computes the same objective to float32 accuracy."""
+    from oracle import fast
+    a, pa, pb = _small_problem(seed=3)
+    rng = np.random.default_rng(2)
+    u = rng.normal(0, 0.3, a["nodes"].shape)
+    J1, g1 = fast.FastProblem(pb, nthreads=2).value_and_grad(u, 0.1)
+    J2, g2 = fast.FastProblem(pb, nthreads=2, precision="f32").value_and_grad(u, 0.1)
+    assert abs(J1 - J2) <= 1e-5 * abs(J1)
+    assert np.abs(g1 - g2).max() <= 1e-4 * np.abs(g1).max()
+
+
 def test_cg_control_flow_quirks():
     """Stop row keeps k; 10 failed halvings apply alpha = 2**-10 anyway (d2ic/solver_global_cg.py:374-459)."""
     calls = {"v": 0}
