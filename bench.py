@@ -60,6 +60,14 @@ def parse():
     p.add_argument("--serve-frames", type=int, default=4)
     p.add_argument("--serve-slots", type=int, default=32)
     p.add_argument("--serve-slice", type=int, default=16)
+    p.add_argument("--no-stream", action="store_true", help="skip the serving stream")
+    p.add_argument("--stream-frames", type=int, default=4096)
+    p.add_argument("--stream-seqs", type=int, default=128)
+    p.add_argument("--stream-plain-frames", type=int, default=4096)
+    p.add_argument("--stream-rates", type=lambda v: [float(x) for x in v.split(",")],
+                   default=[50.0, 100.0, 200.0, 500.0, 1000.0, 2000.0])
+    p.add_argument("--stream-window", type=float, default=20.0,
+                   help="arrivals per rate: the whole stream, or at least 1024 and about this many seconds")
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--batch-frames", type=int, default=64)
     p.add_argument("--batch-sides", default="512,1024,2048,3072,4096",
@@ -417,6 +425,155 @@ def run_serving(args, dev, sides=(512, 1024, 2048), n_seq=None, label="mixed_str
 
 
 # ---------------------------------------------------------------------------
+# the serving stream: Poisson arrivals from many concurrent sequences
+# ---------------------------------------------------------------------------
+
+def _fifo_latency(arrivals, service):
+    """Latencies of a single first-come-first-served server (the plain drop-in handles one frame at
+    a time): frame i starts at max(arrival_i, end of frame i-1) and takes service_i."""
+    t_free, out = 0.0, []
+    for a, sv in zip(arrivals, service):
+        t0 = max(a, t_free)
+        t_free = t0 + sv
+        out.append(t_free - a)
+    return np.asarray(out)
+
+
+def _stream_parity(stream, done, n_check=3):
+    """Served frames against FP64 oracle solves of the same frame from the same warm start (the
+    served result of the sequence's previous frame), on the smallest sequences."""
+    from oracle import fast, objective, pixels
+    out = []
+    seqs = sorted(stream.sequences, key=lambda q: (q.side, -q.element_px))
+    for q in seqs:
+        if len(out) >= n_check:
+            break
+        if (q.seq_id, 1) not in done or (q.seq_id, 0) not in done:
+            continue
+        H = q.side
+        oa = pixels.build_pixel_assets(np.asarray(q.mesh.nodes_xy), np.asarray(q.mesh.elements), H, H,
+                                       q.assets.roi_mask)
+        pb = objective.Problem.build(q.ref.astype(np.float64), q.frames[1].numpy().astype(np.float64), oa)
+        u0 = done[(q.seq_id, 0)].u.astype(np.float64)
+        ur, _, kr, _ = fast.FastProblem(pb).cg_solve(u0, q.config.reg_strength, q.config.max_iters, q.config.tol)
+        r = done[(q.seq_id, 1)]
+        used = np.unique(np.asarray(q.mesh.elements))
+        out.append({"sequence": q.seq_id, "side": H, "element_px": q.element_px, "frame": 1,
+                    "max_err_px": float(np.abs(r.u[used] - ur[used]).max()), "gpu_iters": int(r.n_iters),
+                    "oracle_iters": int(kr)})
+    return out
+
+
+def run_serving_stream(args, dev):
+    """Plain single-frame drop-in vs the continuous-batching server on the serving stream: 4096
+    Poisson arrivals from 128 sequences (sides 512-4096, elements 8-32 px), swept over offered
+    rates; frames are 8-bit camera images in pinned host memory."""
+    import torch
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300 import workloads
+    from d2ic_gb300.serving import DICServer, Request, ServeConfig
+
+    t0 = time.perf_counter()
+    st = workloads.serving_stream(n_arrivals=args.stream_frames, n_seq=args.stream_seqs, device=dev)
+    t_build = time.perf_counter() - t0
+    seqs = st.sequences
+    N = len(st.order)
+    roi = {q.seq_id: q.assets.pixel_data.n_pixels for q in seqs}
+
+    # plain drop-in: one DICMeshBased per sequence, frames one at a time in arrival order
+    t0 = time.perf_counter()
+    dics, inits = {}, {}
+    for q in seqs:
+        dic = d2.DICMeshBased(q.mesh, d2.GlobalCGSolver(device=dev), q.config)
+        dic.prepare(q.ref, q.assets)
+        ini = d2.DICInitMotion(q.init, d2.TranslationZNCCSolver(q.init, device=dev))
+        ini.prepare(q.ref, dic.state.assets)
+        dics[q.seq_id], inits[q.seq_id] = dic, ini
+    t_plain_setup = time.perf_counter() - t0
+
+    def plain(order):
+        prev, svc, out = {}, [], {}
+        for s, k in order:
+            t = time.perf_counter()
+            img = seqs[s].frames[k]
+            dics[s].set_initial_guess(inits[s].run(img).u_nodal if k == 0 else prev[s])
+            r = dics[s].run(img)
+            prev[s] = r.u_nodal
+            svc.append(time.perf_counter() - t)
+            out[(s, k)] = np.asarray(r.u_nodal)
+        return svc, out
+
+    n_plain = min(N, args.stream_plain_frames)
+    plain([(q.seq_id, 0) for q in seqs[:8]])                      # warm-up (lazy device buffers)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    svc, plain_u = plain(st.order[:n_plain])
+    t_plain = time.perf_counter() - t0
+    plain_fps = n_plain / t_plain
+
+    t0 = time.perf_counter()
+    srv = DICServer(dev, ServeConfig(max_slots=min(len(seqs), 128), slice_rounds=args.serve_slice))
+    for q in seqs:
+        srv.add_sequence(q.seq_id, q.ref, q.mesh, q.assets, q.config, init=q.init)
+    t_srv_setup = time.perf_counter() - t0
+
+    def served(n, offsets=None):
+        srv.reset_sequences()
+        reqs = [Request(s, k, seqs[s].frames[k]) for s, k in st.order[:n]]
+        t = time.perf_counter()
+        if offsets is None:
+            for r in reqs:
+                r.t_arrival = t
+                srv.submit(r)
+            srv.run_until_idle()
+        else:
+            srv.run_stream(reqs, offsets)
+        return reqs, time.perf_counter() - t
+
+    served(min(N, 256))                                           # warm-up: graph capture
+    torch.cuda.synchronize()
+    reqs, t_sat = served(N)
+    served_fps = N / t_sat
+    done = {(r.seq_id, r.frame_index): r for r in reqs}
+    diff = max(float(np.abs(done[key].u - u).max()) for key, u in plain_u.items())
+    it_capped = sum(1 for r in reqs if r.n_iters is not None and r.n_iters >= seqs[r.seq_id].config.max_iters)
+    sweep = []
+    for rate in args.stream_rates:
+        n = min(N, max(1024, int(args.stream_window * rate)))
+        offs = st.offsets(rate, n)
+        reqs_k, wall = served(n, offs)
+        lat = np.array([r.latency for r in reqs_k])
+        plain_lat = _fifo_latency(offs[:min(n, n_plain)], svc[:min(n, n_plain)])
+        sweep.append({"offered_frames_per_s": rate, "arrivals": n, "achieved_frames_per_s": n / wall,
+                      "latency_ms_p50": 1000 * float(np.percentile(lat, 50)),
+                      "latency_ms_p99": 1000 * float(np.percentile(lat, 99)),
+                      "plain_latency_ms_p50": 1000 * float(np.percentile(plain_lat, 50)),
+                      "plain_latency_ms_p99": 1000 * float(np.percentile(plain_lat, 99)),
+                      "plain_latency_arrivals": int(len(plain_lat))})
+    parity = _stream_parity(st, done)
+    by_side = {}
+    for q in seqs:
+        by_side.setdefault(q.side, []).append(q.seq_id)
+    return {"workload": "serving_stream", "arrivals": N, "sequences": len(seqs),
+            "image_sides": sorted(by_side), "element_px": sorted({q.element_px for q in seqs}),
+            "sequences_per_side": {str(k): len(v) for k, v in sorted(by_side.items())},
+            "roi_pixels_per_pass": int(sum(roi[s] for s, _ in st.order)), "frame_dtype": "uint8",
+            "host_frame_bytes": st.host_bytes,
+            "plain_frames_per_s": plain_fps, "plain_frames_timed": n_plain,
+            "plain_service_ms_p50": 1000 * float(np.percentile(svc, 50)),
+            "served_frames_per_s": served_fps, "speedup": served_fps / plain_fps,
+            "max_abs_diff_vs_plain_px": diff, "frames_at_max_iters": it_capped,
+            "rate_sweep": sweep, "parity_sampled": parity, "slots": min(len(seqs), 128),
+            "slice_rounds": args.serve_slice, "graphs": sorted(getattr(srv, "graphs", {}) or
+                                                               ({"short": 1} if srv.graph is not None else {})),
+            "setup_s": {"stream": round(t_build, 1), "plain": round(t_plain_setup, 1),
+                        "server": round(t_srv_setup, 1)},
+            "notes": "plain latency per rate: a first-come-first-served queue over the plain drop-in's measured "
+                     "per-frame service times (it solves one frame at a time); served latency measured live"}
+
+
+# ---------------------------------------------------------------------------
 # uneven frames in one persistent launch
 # ---------------------------------------------------------------------------
 
@@ -758,6 +915,8 @@ def run_ours(args, ws, rank, local):
         u_api = np.stack([np.asarray(r.u_nodal) for r in res_b.results])
         out["e2e"]["max_abs_diff_vs_value_path_px"] = float(np.abs(u_dev - u_api).max())
 
+    if not args.no_stream:
+        out["serving_stream"] = run_serving_stream(args, dev)
     if not args.no_serve:
         out["serving"] = run_serving(args, dev)
         # the small-frame regime, where one frame alone cannot fill the GPU

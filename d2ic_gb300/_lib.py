@@ -68,6 +68,10 @@ _SIGS = {
     "d2ic_bspline_prefilter": (i32, [vp, i32, i32, i32, i32, vp, vp, vp]),
     "d2ic_bspline_prefilter_batch": (i32, [vp, i32, i32, i32, i32, i32, vp, vp, vp]),
     "d2ic_pad_image": (i32, [vp, i32, i32, i32, i32, vp, vp]),
+    "d2ic_bspline_prefilter_u8": (i32, [vp, i32, i32, i32, i32, vp, vp, vp]),
+    "d2ic_pad_image_u8": (i32, [vp, i32, i32, i32, i32, vp, vp]),
+    "d2ic_render_speckle": (i32, [vp, vp, f32, i32, i32, f32, vp, i32, i32, vp, vp]),
+    "d2ic_speckle_finish": (i32, [vp, ctypes.c_longlong, f32, f32, f32, ctypes.c_ulonglong, i32, vp, vp]),
     "d2ic_sample_points": (i32, [vp, i32, i32, i32, i32, i32, vp, i32, vp, vp, vp, vp]),
     "d2ic_pack_pixels": (i32, [vp, vp, i32, vp, i32, i32, i32, i32, i32, vp, vp]),
     "d2ic_frame_workspace_bytes": (szt, [i32, i32, i32]),

@@ -34,18 +34,19 @@ static int ensure_fir() {
 }
 
 // rows: tmp[y][cx] = sum_k h[k] img[y][clamp(cx - pad + k)], cx in [0, W + 2 pad); image
-// blockIdx.z of a batch (contiguous images and buffers)
-__global__ void __launch_bounds__(256) prefilter_rows(const float *__restrict__ img, int H, int W, int pad,
+// blockIdx.z of a batch (contiguous images and buffers).  T: float or 8-bit camera pixels.
+template <class T>
+__global__ void __launch_bounds__(256) prefilter_rows(const T *__restrict__ img, int H, int W, int pad,
                                                       int cpitch, float *__restrict__ tmp) {
     __shared__ float s[256 + 2 * KF];
     img += (size_t)blockIdx.z * H * W;
     tmp += (size_t)blockIdx.z * H * cpitch;
     const int y = blockIdx.y;
     const int cx0 = blockIdx.x * 256;
-    const float *row = img + (size_t)y * W;
+    const T *row = img + (size_t)y * W;
     for (int i = threadIdx.x; i < 256 + 2 * KF; i += 256) {
         const int src = clampi(cx0 - pad - KF + i, 0, W - 1);
-        s[i] = __ldg(row + src);
+        s[i] = (float)__ldg(row + src);
     }
     __syncthreads();
     const int cx = cx0 + threadIdx.x;
@@ -83,13 +84,42 @@ __global__ void __launch_bounds__(256) prefilter_cols(const float *__restrict__ 
     }
 }
 
-__global__ void pad_image_kernel(const float *__restrict__ img, int H, int W, int pad, int cpitch,
+template <class T>
+__global__ void pad_image_kernel(const T *__restrict__ img, int H, int W, int pad, int cpitch,
                                  float *__restrict__ out) {
     const int cx = blockIdx.x * blockDim.x + threadIdx.x;
     const int cy = blockIdx.y;
     if (cx >= W + 2 * pad) return;
     const int sy = clampi(cy - pad, 0, H - 1), sx = clampi(cx - pad, 0, W - 1);
-    out[(size_t)cy * cpitch + cx] = __ldg(img + (size_t)sy * W + sx);
+    out[(size_t)cy * cpitch + cx] = (float)__ldg(img + (size_t)sy * W + sx);
+}
+
+template <class T>
+static int prefilter_one(const T *img, int H, int W, int pad, int cpitch, float *tmp, float *coeff, cudaStream_t s,
+                         const char *name) {
+    D2IC_REQUIRE(img && tmp && coeff, "%s: null pointer", name);
+    D2IC_REQUIRE(H > 0 && W > 0 && H < 65536 && W < 65536, "%s: bad image size %dx%d", name, H, W);
+    D2IC_REQUIRE(pad >= KF && cpitch >= W + 2 * pad, "%s: need pad >= %d and cpitch >= W + 2 pad", name, KF);
+    int st = ensure_fir();
+    if (st) return st;
+    const int CW = W + 2 * pad;
+    prefilter_rows<T><<<dim3((CW + 255) / 256, H), 256, 0, s>>>(img, H, W, pad, cpitch, tmp);
+    D2IC_CHECK_LAUNCH("prefilter_rows");
+    prefilter_cols<<<dim3((CW + CT_W - 1) / CT_W, (H + 2 * pad + CT_H - 1) / CT_H), dim3(CT_W, 8), 0, s>>>(
+        tmp, H, W, pad, cpitch, coeff);
+    D2IC_CHECK_LAUNCH("prefilter_cols");
+    return D2IC_OK;
+}
+
+template <class T>
+static int pad_one(const T *img, int H, int W, int pad, int cpitch, float *out, cudaStream_t s, const char *name) {
+    D2IC_REQUIRE(img && out, "%s: null pointer", name);
+    D2IC_REQUIRE(H > 0 && W > 0 && H < 65536 && W < 65536, "%s: bad image size %dx%d", name, H, W);
+    D2IC_REQUIRE(pad >= 0 && cpitch >= W + 2 * pad, "%s: need cpitch >= W + 2 pad", name);
+    const int CW = W + 2 * pad;
+    pad_image_kernel<T><<<dim3((CW + 255) / 256, H + 2 * pad), 256, 0, s>>>(img, H, W, pad, cpitch, out);
+    D2IC_CHECK_LAUNCH("pad_image");
+    return D2IC_OK;
 }
 
 template <int KIND>
@@ -134,7 +164,7 @@ extern "C" int d2ic_bspline_prefilter_batch(const float *img, int n_images, int 
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
     const int CW = W + 2 * pad;
-    prefilter_rows<<<dim3((CW + 255) / 256, H, n_images), 256, 0, s>>>(img, H, W, pad, cpitch, tmp);
+    prefilter_rows<float><<<dim3((CW + 255) / 256, H, n_images), 256, 0, s>>>(img, H, W, pad, cpitch, tmp);
     D2IC_CHECK_LAUNCH("prefilter_rows");
     prefilter_cols<<<dim3((CW + CT_W - 1) / CT_W, (H + 2 * pad + CT_H - 1) / CT_H, n_images), dim3(CT_W, 8), 0, s>>>(
         tmp, H, W, pad, cpitch, coeff);
@@ -144,29 +174,21 @@ extern "C" int d2ic_bspline_prefilter_batch(const float *img, int n_images, int 
 
 extern "C" int d2ic_bspline_prefilter(const float *img, int H, int W, int pad, int cpitch, float *tmp,
                                       float *coeff, void *stream) {
-    D2IC_REQUIRE(img && tmp && coeff, "d2ic_bspline_prefilter: null pointer");
-    D2IC_REQUIRE(H > 0 && W > 0 && H < 65536 && W < 65536, "d2ic_bspline_prefilter: bad image size %dx%d", H, W);
-    D2IC_REQUIRE(pad >= KF && cpitch >= W + 2 * pad, "d2ic_bspline_prefilter: need pad >= %d and cpitch >= W + 2 pad", KF);
-    int st = ensure_fir();
-    if (st) return st;
-    cudaStream_t s = (cudaStream_t)stream;
-    const int CW = W + 2 * pad;
-    prefilter_rows<<<dim3((CW + 255) / 256, H), 256, 0, s>>>(img, H, W, pad, cpitch, tmp);
-    D2IC_CHECK_LAUNCH("prefilter_rows");
-    prefilter_cols<<<dim3((CW + CT_W - 1) / CT_W, (H + 2 * pad + CT_H - 1) / CT_H), dim3(CT_W, 8), 0, s>>>(
-        tmp, H, W, pad, cpitch, coeff);
-    D2IC_CHECK_LAUNCH("prefilter_cols");
-    return D2IC_OK;
+    return prefilter_one(img, H, W, pad, cpitch, tmp, coeff, (cudaStream_t)stream, "d2ic_bspline_prefilter");
+}
+
+extern "C" int d2ic_bspline_prefilter_u8(const unsigned char *img, int H, int W, int pad, int cpitch, float *tmp,
+                                         float *coeff, void *stream) {
+    return prefilter_one(img, H, W, pad, cpitch, tmp, coeff, (cudaStream_t)stream, "d2ic_bspline_prefilter_u8");
 }
 
 extern "C" int d2ic_pad_image(const float *img, int H, int W, int pad, int cpitch, float *out, void *stream) {
-    D2IC_REQUIRE(img && out, "d2ic_pad_image: null pointer");
-    D2IC_REQUIRE(H > 0 && W > 0 && H < 65536 && W < 65536, "d2ic_pad_image: bad image size %dx%d", H, W);
-    D2IC_REQUIRE(pad >= 0 && cpitch >= W + 2 * pad, "d2ic_pad_image: need cpitch >= W + 2 pad");
-    const int CW = W + 2 * pad;
-    pad_image_kernel<<<dim3((CW + 255) / 256, H + 2 * pad), 256, 0, (cudaStream_t)stream>>>(img, H, W, pad, cpitch, out);
-    D2IC_CHECK_LAUNCH("pad_image");
-    return D2IC_OK;
+    return pad_one(img, H, W, pad, cpitch, out, (cudaStream_t)stream, "d2ic_pad_image");
+}
+
+extern "C" int d2ic_pad_image_u8(const unsigned char *img, int H, int W, int pad, int cpitch, float *out,
+                                 void *stream) {
+    return pad_one(img, H, W, pad, cpitch, out, (cudaStream_t)stream, "d2ic_pad_image_u8");
 }
 
 extern "C" int d2ic_sample_points(const float *coeff, int H, int W, int pad, int cpitch, int kind, const float *xy,

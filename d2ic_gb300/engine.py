@@ -50,12 +50,20 @@ def interp_kind(interpolation: str) -> int:
     raise ValueError(f"Unsupported interpolation: {interpolation}")
 
 
-def as_device_image(img, device) -> torch.Tensor:
-    """float32 contiguous (H, W) image on ``device`` (host arrays are copied)."""
+def as_device_image(img, device, keep_u8: bool = False) -> torch.Tensor:
+    """float32 contiguous (H, W) image on ``device`` (host arrays are copied).
+
+    ``keep_u8``: 8-bit camera frames stay 8-bit (one byte per pixel over the host link); the
+    coefficient preparation widens them on the device."""
     if isinstance(img, torch.Tensor):
-        t = img.to(device=device, dtype=torch.float32)
+        if keep_u8 and img.dtype == torch.uint8:
+            t = img.to(device=device, non_blocking=img.device.type == "cpu" and img.is_pinned())
+        else:
+            t = img.to(device=device, dtype=torch.float32)
     else:
-        a = np.asarray(img, dtype=np.float32)
+        a = np.asarray(img)
+        if not (keep_u8 and a.dtype == np.uint8):
+            a = a.astype(np.float32, copy=False)
         t = torch.from_numpy(np.ascontiguousarray(a)).to(device, non_blocking=False)
     if t.dim() != 2:
         raise ValueError(f"expected a 2D image, got shape {tuple(t.shape)}")
@@ -71,12 +79,16 @@ def prepare_coefficients(img_dev: torch.Tensor, kind: int, out: torch.Tensor | N
     if out is None:
         out = torch.empty((H + 2 * PAD, cp), dtype=torch.float32, device=dev)
     s = _lib.stream_handle(stream)
+    u8 = img_dev.dtype == torch.uint8
+    if not u8 and img_dev.dtype != torch.float32:
+        raise ValueError(f"images are float32 or uint8, got {img_dev.dtype}")
     if kind == _lib.INTERP_CUBIC:
         if tmp is None:
             tmp = torch.empty((H, cp), dtype=torch.float32, device=dev)
-        _lib.call("d2ic_bspline_prefilter", ptr(img_dev), H, W, PAD, cp, ptr(tmp), ptr(out), s)
+        _lib.call("d2ic_bspline_prefilter_u8" if u8 else "d2ic_bspline_prefilter", ptr(img_dev), H, W, PAD, cp,
+                  ptr(tmp), ptr(out), s)
     else:
-        _lib.call("d2ic_pad_image", ptr(img_dev), H, W, PAD, cp, ptr(out), s)
+        _lib.call("d2ic_pad_image_u8" if u8 else "d2ic_pad_image", ptr(img_dev), H, W, PAD, cp, ptr(out), s)
     return out
 
 
@@ -305,7 +317,7 @@ class FrameSlot:
         self.desc.alpha_reg = float(alpha_reg)
 
     def load_image(self, def_image, stream=None):
-        img = as_device_image(def_image, self.layout.device)
+        img = as_device_image(def_image, self.layout.device, keep_u8=True)
         prepare_coefficients(img, self.layout.kind, self.coeff, self.tmp, stream)
 
     def set_u0(self, u0):

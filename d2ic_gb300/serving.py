@@ -250,12 +250,15 @@ class DICServer:
             i = free_slots.pop(0)
             slot = seq.slot
             # image: pinned host -> device on the copy stream, then coefficients on the compute stream
+            # (8-bit camera frames cross the host link as bytes and are widened by the prefilter)
             if isinstance(req.image, torch.Tensor) and req.image.is_cuda:
-                img = req.image.to(torch.float32)
+                img = req.image if req.image.dtype == torch.uint8 else req.image.to(torch.float32)
             else:
-                src = req.image if isinstance(req.image, torch.Tensor) else torch.from_numpy(
-                    np.ascontiguousarray(req.image, dtype=np.float32))
-                img = torch.empty((L.H, L.W), dtype=torch.float32, device=self.device)
+                src = req.image if isinstance(req.image, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(
+                    req.image if np.asarray(req.image).dtype == np.uint8 else np.asarray(req.image, np.float32)))
+                if src.dtype != torch.uint8:
+                    src = src.to(torch.float32)
+                img = torch.empty((L.H, L.W), dtype=src.dtype, device=self.device)
                 with torch.cuda.stream(self.copy_stream):
                     img.copy_(src, non_blocking=True)
                 stream.wait_stream(self.copy_stream)

@@ -199,6 +199,82 @@ def speckle_sequence(H: int, W: int, warps, seed: int, noise_seeds, noise_sigma:
 
 
 # ---------------------------------------------------------------------------
+# device rendering (benchmark streams): the same dot field and cut-off, FP32 sums
+# in a fixed order per pixel, affine maps only
+# ---------------------------------------------------------------------------
+
+def _inverse_affine6(warp) -> np.ndarray:
+    """``x = phi^{-1}(y)`` as ``(m0, m1, m2, m3, m4, m5)``: x = m0 + m1 yx + m2 yy, y = m3 + m4 yx + m5 yy."""
+    if warp is None:
+        M, off = np.eye(2), np.zeros(2)
+    elif isinstance(warp, Translation):
+        M, off = np.eye(2), -np.asarray(warp.t, np.float64)
+    elif isinstance(warp, Affine):
+        M = warp.Minv
+        off = warp.x0 - M @ (warp.x0 + warp.t)
+    else:
+        raise ValueError("device rendering supports Translation and Affine maps")
+    return np.array([off[0], M[0, 0], M[0, 1], off[1], M[1, 0], M[1, 1]], np.float64)
+
+
+class DeviceSpeckle:
+    """A dot field bucketed on the host into cells of ``cell_px`` pixels and kept on the device;
+    renders raw fields (``d2ic_render_speckle``) and finished grey-level frames."""
+
+    def __init__(self, H: int, W: int, dots: DotField, device, cell_px: float = 16.0):
+        from . import _lib
+        self.H, self.W, self.device = H, W, torch.device(device)
+        if cell_px < CUTOFF_SIGMAS * float(dots.sigma.max()):
+            raise ValueError("cells must be at least as wide as the largest cut-off radius")
+        gw, gh = int(math.ceil(W / cell_px)) + 1, int(math.ceil(H / cell_px)) + 1
+        cx = np.minimum((dots.cx // cell_px).astype(np.int64), gw - 1)
+        cy = np.minimum((dots.cy // cell_px).astype(np.int64), gh - 1)
+        cell = cy * gw + cx
+        order = np.argsort(cell, kind="stable")
+        start = np.zeros(gw * gh + 1, np.int32)
+        start[1:] = np.cumsum(np.bincount(cell, minlength=gw * gh))
+        d4 = np.stack([dots.cx, dots.cy, dots.sigma, dots.amp], axis=1)[order].astype(np.float32)
+        self.dots = torch.from_numpy(np.ascontiguousarray(d4)).to(self.device)
+        self.start = torch.from_numpy(start).to(self.device)
+        self.gw, self.gh, self.cell_px = gw, gh, float(cell_px)
+        self._lib = _lib
+
+    def raw(self, warp=None, out: torch.Tensor | None = None) -> torch.Tensor:
+        import ctypes
+
+        from ._lib import ptr
+        out = torch.empty((self.H, self.W), dtype=torch.float32, device=self.device) if out is None else out
+        m = np.ascontiguousarray(_inverse_affine6(warp), dtype=np.float64)     # host array: read by the host
+        self._lib.call("d2ic_render_speckle", ptr(self.dots), ptr(self.start), self.cell_px, self.gw, self.gh,
+                       CUTOFF_SIGMAS, m.ctypes.data_as(ctypes.c_void_p), self.H, self.W, ptr(out),
+                       self._lib.stream_handle())
+        return out
+
+    def finish(self, raw: torch.Tensor, lo: float, scale: float, sigma: float, seed: int, u8: bool) -> torch.Tensor:
+        from ._lib import ptr
+        out = torch.empty(raw.shape, dtype=torch.uint8 if u8 else torch.float32, device=self.device)
+        self._lib.call("d2ic_speckle_finish", ptr(raw), raw.numel(), float(lo), float(scale), float(sigma),
+                       int(seed) & 0xFFFFFFFFFFFFFFFF, int(u8), ptr(out), self._lib.stream_handle())
+        return out
+
+
+def speckle_sequence_device(H: int, W: int, warps, seed: int, noise_seeds, noise_sigma: float = 0.5,
+                            device="cuda", u8: bool = True):
+    """Reference image and deformed frames rendered on the device (device tensors).
+
+    Same dot field (seed ``seed``), cut-off and grey-level scaling as :func:`speckle_sequence`;
+    the noise comes from the device generator seeded by ``noise_seeds`` and, with ``u8``, frames
+    are rounded to 8-bit camera pixels."""
+    sp = DeviceSpeckle(H, W, make_dots(H, W, seed), device)
+    raw = sp.raw(None)
+    lo, hi = (float(v) for v in torch.aminmax(raw))
+    scale = 210.0 / max(hi - lo, 1e-12)
+    ref = sp.finish(raw, lo, scale, noise_sigma, noise_seeds[0], u8)
+    frames = [sp.finish(sp.raw(w, raw), lo, scale, noise_sigma, noise_seeds[k + 1], u8) for k, w in enumerate(warps)]
+    return ref, frames
+
+
+# ---------------------------------------------------------------------------
 # benchmark masks
 # ---------------------------------------------------------------------------
 

@@ -109,6 +109,110 @@ def mixed_stream(n_seq: int = 16, frames_per_seq: int = 4, seed: int = 4, device
             for (s, H, elem, ref, frames, mask, warps), (mesh, assets) in zip(specs, built)]
 
 
+@dataclass
+class StreamSequence:
+    """One sequence of the serving stream: reference image (uint8, host), mesh and assets, and
+    its frames (uint8, pinned host tensors) in the order they arrive."""
+    seq_id: int
+    side: int
+    element_px: int
+    ref: np.ndarray
+    mesh: object
+    assets: object
+    frames: list
+    config: MeshDICConfig
+    init: InitMotionConfig
+    warps: list
+
+
+@dataclass
+class ServingStream:
+    """Arrival order of a serving stream: ``order[i] = (sequence, frame index)`` of arrival i."""
+    sequences: list
+    order: list
+    seed: int
+
+    def offsets(self, rate: float, n: int | None = None, seed: int | None = None) -> np.ndarray:
+        """Poisson arrival times (seconds from the start) of the first ``n`` arrivals at ``rate``."""
+        n = len(self.order) if n is None else n
+        rng = np.random.default_rng((self.seed if seed is None else seed) * 100003 + int(round(rate)))
+        return np.cumsum(rng.exponential(1.0 / rate, n))
+
+    @property
+    def host_bytes(self) -> int:
+        return sum(int(f.numel()) for s in self.sequences for f in s.frames)
+
+
+def serving_stream(n_arrivals: int = 4096, n_seq: int = 128, seed: int = 4, device="cuda",
+                   sides=(512, 1024, 2048, 4096), elements=(8, 16, 32), noise_sigma: float = 0.5,
+                   pin: bool = True, device_assets: bool = True) -> ServingStream:
+    """The serving stream: ``n_arrivals`` frames from ``n_seq`` concurrent sequences.
+
+    Seed ``seed`` draws each sequence's image side and element size (uniform over ``sides`` and
+    ``elements``), then the sequence of every arrival (uniform over sequences; a sequence's
+    frames arrive in order).  Sequence s uses seed ``4000 + s`` for its speckle, its ellipse mask
+    (40-90% of the image) and its random affine map (strains +-2%, rotation +-1 deg, translation
+    +-3 px about the centre), reached linearly over its frames: frame k of F shows the map at
+    fraction (k + 1) / F.  Frames are 8-bit camera images with N(0, noise_sigma^2) grey noise,
+    rendered on the device and kept in pinned host memory; frame 0 of a sequence is initialised
+    by ZNCC + IDW, later frames warm-start from the previous solution.  ``device_assets``: pixel
+    assets as device-layout recipes (build_pixel_assets_device) instead of host arrays."""
+    import math
+    from dataclasses import replace
+
+    import torch
+
+    from .synthetic import Affine, ellipse_mask, speckle_sequence_device
+    rng = np.random.default_rng(seed)
+    side = [int(rng.choice(sides)) for _ in range(n_seq)]
+    elem = [int(rng.choice(elements)) for _ in range(n_seq)]
+    seq_of = rng.integers(0, n_seq, n_arrivals)
+    counts = np.bincount(seq_of, minlength=n_seq)
+    order, seen = [], np.zeros(n_seq, np.int64)
+    for s in seq_of:
+        order.append((int(s), int(seen[s])))
+        seen[s] += 1
+    specs = []
+    for s in range(n_seq):
+        H, F = side[s], max(int(counts[s]), 1)
+        r = np.random.default_rng(4000 + s)
+        exx, eyy, exy = r.uniform(-0.02, 0.02, 3)
+        th = math.radians(r.uniform(-1.0, 1.0))
+        t = r.uniform(-3.0, 3.0, 2)
+        A = np.array([[exx, exy], [exy, eyy]]) + np.array([[math.cos(th) - 1, -math.sin(th)],
+                                                          [math.sin(th), math.cos(th) - 1]])
+        warps = [Affine(A * (k + 1) / F, t * (k + 1) / F, [H / 2, H / 2]) for k in range(int(counts[s]))]
+        ref_d, frames_d = speckle_sequence_device(H, H, warps, seed=4000 + s,
+                                                  noise_seeds=[4_000_000 + 10_000 * s + k for k in range(len(warps) + 1)],
+                                                  noise_sigma=noise_sigma, device=device, u8=True)
+        frames = []
+        for f in frames_d:
+            h = torch.empty(f.shape, dtype=torch.uint8, pin_memory=pin)
+            h.copy_(f)
+            frames.append(h)
+        ref = ref_d.cpu().numpy()
+        specs.append((s, H, elem[s], ref, frames, ellipse_mask(H, H, r), warps))
+    built = None
+    if device_assets:
+        try:
+            from .pixel_assets import build_pixel_assets_device
+        except ImportError:
+            build_pixel_assets_device = None
+        if build_pixel_assets_device is not None:
+            built = []
+            for sp in specs:
+                mesh, assets = mask_to_mesh_assets(sp[5], sp[2])
+                built.append((mesh, replace(assets, pixel_data=build_pixel_assets_device(mesh, sp[3], 1.0,
+                                                                                          assets.roi_mask))))
+    if built is None:
+        built = _build_assets([(sp[5], sp[3].astype(np.float32)) for sp in specs], [sp[2] for sp in specs])
+    seqs = [StreamSequence(s, H, e, ref, mesh, assets, frames,
+                           MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1),
+                           InitMotionConfig(win=17, search=8, score_min=0.2), warps)
+            for (s, H, e, ref, frames, mask, warps), (mesh, assets) in zip(specs, built)]
+    return ServingStream(seqs, order, seed)
+
+
 def plate_hole_2048(n_frames: int = 20, seed: int = 1, device="cpu", H: int = 2048) -> Workload:
     W = H
     s = H / 2048.0

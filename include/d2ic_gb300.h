@@ -140,6 +140,14 @@ D2IC_API int d2ic_bspline_prefilter_batch(const float *img, int n_images, int H,
 /* Copy an image into the halo layout with edge replication (linear kind). */
 D2IC_API int d2ic_pad_image(const float *img, int H, int W, int pad, int cpitch, float *out, void *stream);
 
+/* The same two preparations for 8-bit camera frames (GlobalCGSolver.solve takes the frame as given,
+ * jnp.asarray(def_image), d2ic/solver_global_cg.py:157-159): the pixels are read as uint8 and
+ * widened on the device, so a frame crosses the host link at one byte per pixel. */
+D2IC_API int d2ic_bspline_prefilter_u8(const unsigned char *img, int H, int W, int pad, int cpitch,
+                                       float *tmp, float *coeff, void *stream);
+D2IC_API int d2ic_pad_image_u8(const unsigned char *img, int H, int W, int pad, int cpitch, float *out,
+                               void *stream);
+
 
 /* Sample n points at image-index coordinates xy (x = col, y = row, i.e. the
  * reference's pixel-centre coordinates minus 0.5); value and d/dx, d/dy.
@@ -335,6 +343,23 @@ D2IC_API int d2ic_mixed_term_T(const d2ic_frame_t *frame_dev, int n_chunks, cons
  * tmp: H x cpitch floats. */
 D2IC_API int d2ic_bspline_prefilter_T(const float *gcoeff, int H, int W, int pad, int cpitch, float *tmp, float *gimg,
                                       void *stream);
+
+/* ---- synthetic speckle frames (no counterpart in the reference, which reads camera images from
+ *      disk): the benchmark streams' stand-in for recorded frames ---- */
+
+/* Raw speckle field at every pixel centre y of an HxW frame: sum over dots (cx, cy, sigma, amp;
+ * float4 each, bucketed by cell of `cell_px` pixels, gw x gh cells row-major, dots of cell c at
+ * cell_start[c] .. cell_start[c+1]-1) of amp exp(-|x - c|^2 / (2 sigma^2)) for
+ * |x - c| <= cutoff_sigmas sigma, at x = phi^-1(y) given as 6 doubles in HOST memory (x = m0 + m1 yx
+ * + m2 yy, y = m3 + m4 yx + m5 yy); dots, cell_start and out are device pointers.  cell_px must be at
+ * least the largest cut-off radius. */
+D2IC_API int d2ic_render_speckle(const float *dots, const int *cell_start, float cell_px, int gw, int gh,
+                                 float cutoff_sigmas, const double *inv_affine, int H, int W, float *out,
+                                 void *stream);
+/* Grey levels 20 + (raw - lo) scale plus N(0, sigma^2) noise from a counter-based generator seeded by
+ * `seed`; out is float32, or uint8 rounded and clamped to [0, 255] when out_u8 != 0. */
+D2IC_API int d2ic_speckle_finish(const float *raw, long long n, float lo, float scale, float sigma,
+                                 unsigned long long seed, int out_u8, void *out, void *stream);
 
 /* ---- initial motion (replaces _match_centers_jax, d2ic/solver_translation_zncc.py:118-168,
  *      and _project_centers_to_nodes_idw, d2ic/dic_init_motion.py:64-91) ---- */
