@@ -421,7 +421,7 @@ def run_serving(args, dev, sides=(512, 1024, 2048), n_seq=None, label="mixed_str
             "plain_latency_ms_p99": 1000 * float(np.percentile(plain_lat, 99)),
             "online_rate_frames_per_s": rate, "latency_ms_p50": sweep[1]["latency_ms_p50"],
             "latency_ms_p99": sweep[1]["latency_ms_p99"], "rate_sweep": sweep, "slots": args.serve_slots,
-            "slice_rounds": args.serve_slice, "graphs": srv.graph is not None}
+            "slice_rounds": args.serve_slice, "graphs": sorted(srv.graphs)}
 
 
 # ---------------------------------------------------------------------------
@@ -565,8 +565,7 @@ def run_serving_stream(args, dev):
             "served_frames_per_s": served_fps, "speedup": served_fps / plain_fps,
             "max_abs_diff_vs_plain_px": diff, "frames_at_max_iters": it_capped,
             "rate_sweep": sweep, "parity_sampled": parity, "slots": min(len(seqs), 128),
-            "slice_rounds": args.serve_slice, "graphs": sorted(getattr(srv, "graphs", {}) or
-                                                               ({"short": 1} if srv.graph is not None else {})),
+            "slice_rounds": args.serve_slice, "graphs": sorted(srv.graphs), "long_slices": srv.long_slices,
             "setup_s": {"stream": round(t_build, 1), "plain": round(t_plain_setup, 1),
                         "server": round(t_srv_setup, 1)},
             "notes": "plain latency per rate: a first-come-first-served queue over the plain drop-in's measured "

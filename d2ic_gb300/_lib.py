@@ -25,6 +25,7 @@ CUDA_ERROR = -6
 UNSUPPORTED = -7
 RUNNING = 1
 CMD_INIT, CMD_RUN, CMD_IDLE = 0, 1, 2
+STOP_ON_FINISH, STOP_ON_IRQ = 1, 2
 
 INTERP_CUBIC = 0
 INTERP_LINEAR = 1
@@ -83,6 +84,8 @@ _SIGS = {
     "d2ic_cg_solve_noalloc": (i32, [vp, i32, vp]),
     "d2ic_cg_command_offset": (szt, []),
     "d2ic_cg_slice": (i32, [vp, i32, vp, szt, i32, i32, i32, vp]),
+    "d2ic_cg_slice_ex": (i32, [vp, i32, vp, szt, i32, i32, i32, i32, vp]),
+    "d2ic_cg_irq_offset": (szt, []),
     "d2ic_eval_objective": (i32, [vp, vp, vp, szt, i32, vp, vp, vp]),
     "d2ic_hessian_chunks": (i32, [vp, i32, vp, i32, vp, vp]),
     "d2ic_hessian_matvec": (i32, [vp, i32, i32, vp, vp, i32, f32, f32, vp, vp, vp]),

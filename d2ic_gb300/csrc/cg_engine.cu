@@ -89,8 +89,15 @@ struct CtlHeader {
     int finished;           // a frame finished in this round: the active list is rebuilt before release
     int max_rounds;
     int frames_done;        // frames whose control step ran in the current round
-    int pad_[5];
+    int slice_stop;         // the slice ends after the released round (set before the release)
+    int irq;                // written by the host while a slice runs: end the slice at the next round end
+    int pad_[3];
 };
+static_assert(sizeof(CtlHeader) == 64, "control header layout");
+
+// stop_flags of a slice: end it early
+enum { STOP_ON_FINISH = D2IC_STOP_ON_FINISH,   // after a round in which a frame finished
+       STOP_ON_IRQ = D2IC_STOP_ON_IRQ };         // after a round that ends with the header's irq word set
 
 struct Ctl {
     CtlHeader *h;
@@ -1006,7 +1013,7 @@ template <int KIND, bool ONE = false>
 __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_frame_t *__restrict__ frames, int n_frames,
                                                    char *ctl_base, int eval_only, const float *u_eval,
                                                    double *J_out, float *grad_out, unsigned long long *trace,
-                                                   int trace_rounds, int max_rounds) {
+                                                   int trace_rounds, int max_rounds, int stop_flags) {
     __shared__ unsigned long long s_bar[NWARP][2];   // per-warp mbarriers of the two record buffers
     // per warp and buffer: the nodal candidate inputs of the staged chunk, u of node a at [a], g at
     // [4 + a], the previous direction at [8 + a] (cp.async, completing on the buffer's mbarrier)
@@ -1015,7 +1022,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     __shared__ int s_gpre[FCACHE + 1];
     __shared__ int s_act[FCACHE];
     __shared__ FInfo s_fi[FCACHE];
-    __shared__ int s_hdr[4];                         // n_active, total_chunks, total_groups, abort
+    __shared__ int s_hdr[5];                         // n_active, total_chunks, total_groups, abort, slice_stop
     __shared__ DF s_gq[NWARP][D2IC_NPART];           // group partials of this block's supergroup
     __shared__ int s_sgcnt;                          // groups of this block's supergroup reduced this round
     // per warp: two record buffers, then two coefficient-tile buffers (all 128-byte aligned)
@@ -1091,6 +1098,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         s_hdr[1] = ld_vol(&C.h->total_chunks);
         s_hdr[2] = ld_vol(&C.h->total_groups);
         s_hdr[3] = ld_vol(&C.h->abort);
+        s_hdr[4] = 0;
     }
     __syncthreads();
     load_list(C, s_hdr[0], s_cpre, s_gpre, s_act, s_fi);
@@ -1100,7 +1108,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         const int na = s_hdr[0];
         const int total = s_hdr[1];
         const int tg = s_hdr[2];
-        if (na == 0 || s_hdr[3]) break;
+        if (na == 0 || s_hdr[3] || s_hdr[4]) break;
         const bool trr = tr && round < trace_rounds;
         if (trr) trace[7 * round + 0] = gtimer();
         // the active list only shrinks within a launch: the same count means the same list
@@ -1394,10 +1402,14 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                             // every frame of the round has run its control step, so every block's
                             // work of the round is done: rebuild the active list and release the round
                             if (lane == 0) C.h->frames_done = 0;
+                            int stop = 0;
                             if (ld_vol(&C.h->finished)) {
                                 rebuild_active_warp(frames, n_frames, C, lane);
                                 if (lane == 0) C.h->finished = 0;
+                                stop = stop_flags & STOP_ON_FINISH;
                             }
+                            if (lane == 0 && (stop || ((stop_flags & STOP_ON_IRQ) && ld_vol(&C.h->irq))))
+                                C.h->slice_stop = 1;   // published by the release below
                             __syncwarp();
                             if (lane == 0) {
                                 __threadfence();
@@ -1448,6 +1460,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             s_hdr[1] = ld_vol(&C.h->total_chunks);
             s_hdr[2] = ld_vol(&C.h->total_groups);
             s_hdr[3] = ld_vol(&C.h->abort);
+            s_hdr[4] = ld_vol(&C.h->slice_stop);
         }
         if (na <= FCACHE)
             for (int s = threadIdx.x; s < na; s += NT) s_fi[s] = frame_info(C.fs + s_act[s]);
@@ -1542,7 +1555,7 @@ static int dev_info(int dev, DevInfo **out) {
 static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes, int kind,
                          int grid_blocks, int eval_only, const float *u_eval, double *J_out, float *grad_out,
                          unsigned long long *trace, int trace_rounds, cudaStream_t s, int max_rounds = 0x7fffffff,
-                         bool new_batch = true) {
+                         bool new_batch = true, int stop_flags = 0) {
     D2IC_REQUIRE(frames && control, "cg engine: null pointer");
     D2IC_REQUIRE(n_frames >= 1 && n_frames <= D2IC_MAX_FRAMES, "cg engine: n_frames %d out of [1, %d]", n_frames,
                  D2IC_MAX_FRAMES);
@@ -1578,14 +1591,14 @@ static int launch_engine(const d2ic_frame_t *frames, int n_frames, void *control
     const bool one = n_frames == 1;
     if (kind == D2IC_INTERP_CUBIC)
         e = one ? cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_CUBIC, true>, frames, n_frames, cb, eval_only, u_eval,
-                                     J_out, grad_out, trace, trace_rounds, max_rounds)
+                                     J_out, grad_out, trace, trace_rounds, max_rounds, stop_flags)
                 : cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_CUBIC>, frames, n_frames, cb, eval_only, u_eval, J_out,
-                                     grad_out, trace, trace_rounds, max_rounds);
+                                     grad_out, trace, trace_rounds, max_rounds, stop_flags);
     else
         e = one ? cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_LINEAR, true>, frames, n_frames, cb, eval_only,
-                                     u_eval, J_out, grad_out, trace, trace_rounds, max_rounds)
+                                     u_eval, J_out, grad_out, trace, trace_rounds, max_rounds, stop_flags)
                 : cudaLaunchKernelEx(&cfg, cg_engine<D2IC_INTERP_LINEAR>, frames, n_frames, cb, eval_only, u_eval,
-                                     J_out, grad_out, trace, trace_rounds, max_rounds);
+                                     J_out, grad_out, trace, trace_rounds, max_rounds, stop_flags);
     if (e != cudaSuccess) return cuda_status(e, "cooperative launch of cg_engine");
     return D2IC_OK;
 }
@@ -1732,6 +1745,17 @@ extern "C" int d2ic_cg_slice(const d2ic_frame_t *frames, int n_frames, void *con
     return launch_engine(frames, n_frames, control, control_bytes, interp_kind, grid_blocks, 0, nullptr, nullptr,
                          nullptr, nullptr, 0, (cudaStream_t)stream, max_rounds, false);
 }
+
+extern "C" int d2ic_cg_slice_ex(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
+                                int interp_kind, int grid_blocks, int max_rounds, int stop_flags, void *stream) {
+    D2IC_REQUIRE(max_rounds >= 1, "d2ic_cg_slice_ex: max_rounds must be >= 1 (got %d)", max_rounds);
+    D2IC_REQUIRE((stop_flags & ~(D2IC_STOP_ON_FINISH | D2IC_STOP_ON_IRQ)) == 0, "d2ic_cg_slice_ex: unknown stop flags %d",
+                 stop_flags);
+    return launch_engine(frames, n_frames, control, control_bytes, interp_kind, grid_blocks, 0, nullptr, nullptr,
+                         nullptr, nullptr, 0, (cudaStream_t)stream, max_rounds, false, stop_flags);
+}
+
+extern "C" size_t d2ic_cg_irq_offset(void) { return offsetof(CtlHeader, irq); }
 
 extern "C" int d2ic_cg_solve_traced(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
                                     int interp_kind, int grid_blocks, unsigned long long *trace, int trace_rounds,

@@ -358,12 +358,22 @@ class Engine:
         return self.control[off: off + 4 * n_frames].view(torch.int32)
 
     def run_slice(self, desc_dev: torch.Tensor, n_frames: int, kind: int, max_rounds: int, grid_blocks: int = 0,
-                  stream=None):
-        """Advance every admitted frame by at most ``max_rounds`` objective evaluations."""
+                  stream=None, stop_flags: int = 0):
+        """Advance every admitted frame by at most ``max_rounds`` objective evaluations; with
+        ``stop_flags`` (D2IC_STOP_ON_FINISH | D2IC_STOP_ON_IRQ) the slice may end earlier."""
         if n_frames > self.max_frames:
             raise ValueError(f"{n_frames} frames > engine capacity {self.max_frames}")
-        _lib.call("d2ic_cg_slice", ptr(desc_dev), n_frames, ptr(self.control), self.control.numel(), kind,
-                  grid_blocks, int(max_rounds), _lib.stream_handle(stream))
+        if stop_flags:
+            _lib.call("d2ic_cg_slice_ex", ptr(desc_dev), n_frames, ptr(self.control), self.control.numel(), kind,
+                      grid_blocks, int(max_rounds), int(stop_flags), _lib.stream_handle(stream))
+        else:
+            _lib.call("d2ic_cg_slice", ptr(desc_dev), n_frames, ptr(self.control), self.control.numel(), kind,
+                      grid_blocks, int(max_rounds), _lib.stream_handle(stream))
+
+    def irq_word(self) -> torch.Tensor:
+        """The control block's interrupt word (int32 view): non-zero ends a D2IC_STOP_ON_IRQ slice."""
+        off = int(_lib.load().d2ic_cg_irq_offset())
+        return self.control[off:off + 4].view(torch.int32)
 
     def solve_traced(self, desc_dev: torch.Tensor, n_frames: int, kind: int, rounds: int = 4096, grid_blocks: int = 0):
         """Solve; per-round durations in microseconds, columns: warp 0 of block 0's pixel work, its

@@ -64,6 +64,9 @@ class ServeConfig:
     use_graphs: bool = True
     grid_blocks: int = 0
     autotune: bool = False                   # chunk size per sequence from the launch-shape autotuner
+    # light load: with at most this many frames in flight and none waiting, one long slice runs at a
+    # time and ends when a frame finishes or a new request can be admitted (0 turns this off)
+    light_load_frames: int = 4
 
 
 @dataclass
@@ -135,10 +138,23 @@ class DICServer:
         self.budget = int(self.cfg.hbm_budget_bytes or 0.8 * free)
         self.bytes_in_use = 0
         self.copy_stream = torch.cuda.Stream(device=self.device)
-        self.graph = None
+        self.graphs: dict = {}                  # slice mode -> captured CUDA graph
         self.graph_failed = False
         self.slices = 0
         self.busy_time = 0.0
+        # light-load slices: the host interrupts a running slice by writing the control block's irq word
+        # from a side stream (the kernel reads it at each round end; every launch clears it)
+        self.irq_stream = torch.cuda.Stream(device=self.device)
+        self.irq_dev = self.engine.irq_word()
+        self.irq_one = torch.ones(1, dtype=torch.int32).pin_memory()
+        self.irq_sent = False
+        self.long_running = False
+        self.long_slices = 0
+
+    @property
+    def graph(self):
+        """The short-slice graph (None until captured)."""
+        return self.graphs.get("short")
 
     # -- sequences -----------------------------------------------------------------------------------
     def add_sequence(self, seq_id, ref_image, mesh, assets, config: MeshDICConfig,
@@ -291,28 +307,57 @@ class DICServer:
             admitted += 1
         return admitted
 
-    def _launch_slice(self):
+    LONG_ROUNDS = 1 << 20
+
+    def _launch_slice(self, mode: str = "short"):
+        """Queue one slice: ``short`` = slice_rounds rounds; ``long`` = until a frame finishes or the
+        host raises the irq word (light load)."""
         n = self.cfg.max_slots
+        if mode == "long":
+            rounds, flags = self.LONG_ROUNDS, _lib.STOP_ON_FINISH | _lib.STOP_ON_IRQ
+        else:
+            rounds, flags = self.cfg.slice_rounds, 0
 
         def launch():
-            self.engine.run_slice(self.desc_dev, n, self.kind, self.cfg.slice_rounds, self.cfg.grid_blocks)
+            self.engine.run_slice(self.desc_dev, n, self.kind, rounds, self.cfg.grid_blocks, stop_flags=flags)
 
         if self.cfg.use_graphs and not self.graph_failed:
-            if self.graph is None:
+            g = self.graphs.get(mode)
+            if g is None:
                 try:
                     launch()                                 # this slice runs directly; later ones replay
+                    if mode == "long":
+                        return                               # captured at its next use, when no slice runs
                     torch.cuda.synchronize(self.device)
                     g = torch.cuda.CUDAGraph()
                     with torch.cuda.graph(g):
                         launch()
-                    self.graph = g
+                    self.graphs[mode] = g
                 except Exception:
                     self.graph_failed = True
-                    self.graph = None
+                    self.graphs.clear()
                 return
-            self.graph.replay()
+            g.replay()
         else:
             launch()
+
+    def _capture_long(self):
+        """Capture the long-slice graph while nothing runs (a capture launches nothing)."""
+        if not self.cfg.use_graphs or self.graph_failed or "long" in self.graphs or self.slices == 0:
+            return
+        try:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self.engine.run_slice(self.desc_dev, self.cfg.max_slots, self.kind, self.LONG_ROUNDS,
+                                      self.cfg.grid_blocks, stop_flags=_lib.STOP_ON_FINISH | _lib.STOP_ON_IRQ)
+            self.graphs["long"] = g
+        except Exception:
+            self.graph_failed = True
+            self.graphs.clear()
+
+    def _admissible(self) -> bool:
+        """A queued request could be admitted now (a free slot and a sequence with no frame in flight)."""
+        return bool(self.ready) and any(x is None for x in self.slots)
 
     def _harvest(self, parity: int, slice_no: int):
         """Frames that finished by slice ``slice_no`` (status copy of parity ``parity``)."""
@@ -362,23 +407,64 @@ class DICServer:
                 keep.append((req, seq, ev))
         self.awaiting = keep
 
+    def _queue_slice(self, mode: str):
+        self._launch_slice(mode)                    # the kernel turns CMD_INIT into CMD_RUN as it admits
+        p = self.parity
+        self.status_host[p].copy_(self.status_dev, non_blocking=True)
+        self.status_event[p].record()
+        self.pending_slices.append((p, self.slices))
+        self.parity ^= 1
+        self.slices += 1
+
+    def _light(self) -> bool:
+        n = sum(x is not None for x in self.slots)
+        return 0 < n <= self.cfg.light_load_frames and not self._admissible()
+
     def step(self) -> int:
-        """Admit what fits, queue one engine slice, harvest the previous one; returns frames finished."""
-        self._admit()
+        """Admit what fits, queue one engine slice, harvest the previous one; returns frames finished.
+
+        Under load, short slices are queued back to back and each is harvested while the next one
+        runs.  Under light load one long slice runs at a time: it ends when a frame finishes (its
+        result is harvested at once) or when the host raises the irq word because a new request can
+        be admitted, so neither a finished frame nor a new arrival waits for a fixed slice length."""
         done = 0
         t0 = time.perf_counter()
-        if any(x is not None for x in self.slots):
-            self._launch_slice()                    # the kernel turns CMD_INIT into CMD_RUN as it admits
-            p = self.parity
-            self.status_host[p].copy_(self.status_dev, non_blocking=True)
-            self.status_event[p].record()
-            self.pending_slices.append((p, self.slices))
-            self.parity ^= 1
-            self.slices += 1
+        if self.long_running:
+            if not self.status_event[self.pending_slices[0][0]].query():
+                if not self.irq_sent and self._admissible():
+                    with torch.cuda.stream(self.irq_stream):
+                        self.irq_dev.copy_(self.irq_one, non_blocking=True)
+                    self.irq_sent = True
+                self._complete()
+                self.busy_time += time.perf_counter() - t0
+                return 0
+            self.long_running = False
+            done += self._harvest(*self.pending_slices.popleft())
+        self._admit()
+        light = self._light()
+        if light and self.pending_slices:
+            # switching to a long slice: let the queued short slices finish first (without blocking)
+            while self.pending_slices and self.status_event[self.pending_slices[0][0]].query():
+                done += self._harvest(*self.pending_slices.popleft())
+            if self.pending_slices:
+                self._complete()
+                self.busy_time += time.perf_counter() - t0
+                return done
+            self._admit()
+            light = self._light()
+        if self._occupied():
+            if light:
+                self._capture_long()
+                self._queue_slice("long")
+                self.long_running = True
+                self.long_slices += 1
+                self.irq_sent = False
+            else:
+                self._queue_slice("short")
         # harvest the older slice while the newer one runs (at most one slice left unharvested, so
         # the two pinned status buffers never overlap); with no newer slice, harvest the last one
-        while len(self.pending_slices) > 1 or (self.pending_slices and (
-                not self._occupied() or self.status_event[self.pending_slices[0][0]].query())):
+        while not self.long_running and (len(self.pending_slices) > 1 or (self.pending_slices and (
+                not self._occupied() or self.status_event[self.pending_slices[0][0]].query()))):
             done += self._harvest(*self.pending_slices.popleft())
         self._complete()
         self.busy_time += time.perf_counter() - t0
@@ -395,7 +481,8 @@ class DICServer:
 
     def stats(self) -> dict:
         lat = np.array([r.latency for r in self.completed if r.latency is not None])
-        out = {"frames": len(self.completed), "slices": self.slices, "graphs": self.graph is not None}
+        out = {"frames": len(self.completed), "slices": self.slices, "long_slices": self.long_slices,
+               "graphs": sorted(self.graphs)}
         if lat.size:
             out.update(latency_ms_p50=1000 * float(np.percentile(lat, 50)),
                        latency_ms_p99=1000 * float(np.percentile(lat, 99)))

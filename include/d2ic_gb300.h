@@ -276,6 +276,17 @@ D2IC_API size_t d2ic_cg_command_offset(void);
 D2IC_API int d2ic_cg_slice(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
                            int interp_kind, int grid_blocks, int max_rounds, void *stream);
 
+/* d2ic_cg_slice that may end before max_rounds: with D2IC_STOP_ON_FINISH after the first round in
+ * which a frame finishes (its outputs are then written at once), with D2IC_STOP_ON_IRQ after a round
+ * that ends while the 32-bit word at control + d2ic_cg_irq_offset() is non-zero.  The host writes that
+ * word (a copy on another stream) while the slice runs, to admit new frames without waiting for the
+ * slice; every launch clears it.  Lets a lightly loaded server run long slices. */
+#define D2IC_STOP_ON_FINISH 1
+#define D2IC_STOP_ON_IRQ    2
+D2IC_API size_t d2ic_cg_irq_offset(void);
+D2IC_API int d2ic_cg_slice_ex(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
+                              int interp_kind, int grid_blocks, int max_rounds, int stop_flags, void *stream);
+
 
 /* As d2ic_cg_solve_batched, and writes 6 %globaltimer stamps per round into
  * trace[6*r .. 6*r+5] for r < trace_rounds: block 0's round start, end of the

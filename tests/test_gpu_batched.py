@@ -76,8 +76,8 @@ def test_server_equals_plain_sequences(cuda):
             out.append(r)
             u_prev = r.u_nodal
         plain[sid] = out
-    # served: both sequences at once, slices of 7 rounds
-    srv = DICServer(cuda, ServeConfig(max_slots=4, slice_rounds=7))
+    # served: both sequences at once, slices of 7 rounds (short slices only)
+    srv = DICServer(cuda, ServeConfig(max_slots=4, slice_rounds=7, light_load_frames=0))
     for sid, (ref, frames, mesh, assets) in seqs.items():
         srv.add_sequence(sid, ref, mesh, assets, cfg)
     for k in range(3):
@@ -123,3 +123,93 @@ def test_overlapped_sequence_equals_frame_by_frame(cuda):
         assert np.array_equal(np.asarray(a.u_nodal), np.asarray(b.u_nodal))
         assert np.array_equal(np.asarray(a.strain), np.asarray(b.strain))
         assert a.diagnostics.info["n_iters"] == b.diagnostics.info["n_iters"]
+
+
+def _two_sequences():
+    import d2ic_gb300 as d2
+    from d2ic_gb300.synthetic import Translation, rect_mask, speckle_sequence
+    from dataclasses import replace
+    seqs = {}
+    for sid, (H, elem, seed) in enumerate([(192, 16, 51), (256, 12, 52)]):
+        warps = [Translation(0.2 * (k + 1), -0.15 * (k + 1)) for k in range(3)]
+        ref, frames = speckle_sequence(H, H, warps, seed=seed, noise_seeds=[seed, seed + 1, seed + 2, seed + 3])
+        mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, H, H - 32, H - 32), elem)
+        assets = replace(assets, pixel_data=d2.build_pixel_assets(mesh, ref, 1.0, assets.roi_mask))
+        seqs[sid] = (ref, frames, mesh, assets)
+    return seqs
+
+
+def _served(cuda, seqs, cfg, scfg, offsets=None):
+    from d2ic_gb300.serving import DICServer, Request
+    srv = DICServer(cuda, scfg)
+    for sid, (ref, frames, mesh, assets) in seqs.items():
+        srv.add_sequence(sid, ref, mesh, assets, cfg)
+    reqs = [Request(sid, k, seqs[sid][1][k]) for k in range(3) for sid in seqs]
+    if offsets is None:
+        for r in reqs:
+            srv.submit(r)
+        srv.run_until_idle()
+    else:
+        srv.run_stream(reqs, offsets)
+    return srv, {(r.seq_id, r.frame_index): r for r in srv.completed}
+
+
+def test_light_load_slices_equal_short_slices(cuda):
+    """Under light load the server runs one long slice at a time that ends when a frame finishes
+    (D2IC_STOP_ON_FINISH) or when the host raises the irq word for a new arrival
+    (D2IC_STOP_ON_IRQ); the results must be bitwise those of fixed short slices."""
+    import d2ic_gb300 as d2
+    from d2ic_gb300.serving import ServeConfig
+    seqs = _two_sequences()
+    cfg = d2.MeshDICConfig(max_iters=60, tol=1e-4, reg_strength=0.1)
+    _, short = _served(cuda, seqs, cfg, ServeConfig(max_slots=4, slice_rounds=5, light_load_frames=0))
+    # staggered arrivals: frames arrive while others run, so the irq path is taken as well
+    offs = [0.0, 0.001, 0.002, 0.004, 0.006, 0.008]
+    srv, light = _served(cuda, seqs, cfg, ServeConfig(max_slots=4, slice_rounds=5, light_load_frames=4), offs)
+    assert srv.long_slices >= 3
+    assert set(light) == set(short)
+    for key, r in short.items():
+        q = light[key]
+        assert q.n_iters == r.n_iters
+        assert np.array_equal(q.u, r.u)
+        assert np.array_equal(q.strain, r.strain)
+
+
+def test_slice_stops_when_a_frame_finishes(cuda, uneven):
+    """d2ic_cg_slice_ex with D2IC_STOP_ON_FINISH ends after the first round in which a frame
+    finishes: that frame's outputs are written, the others report RUNNING, and continuing in
+    further slices gives bitwise the one-launch result."""
+    import torch
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300 import _lib, engine
+    from d2ic_gb300.serving import solve_batch
+    # different iteration caps, so that the frames finish in different rounds
+    cfgs = [d2.MeshDICConfig(max_iters=m, tol=1e-4, reg_strength=0.1) for m in (30, 55, 80)]
+    layouts = [engine.FrameLayout(pix, mesh.nodes_xy.shape[0], ref, "cubic", cuda)
+               for ref, dfm, mesh, assets, pix in uneven]
+    one = solve_batch([(L, c[1], None, cfg) for L, c, cfg in zip(layouts, uneven, cfgs)], cuda)
+    slots = []
+    for L, c, cfg in zip(layouts, uneven, cfgs):
+        s = engine.FrameSlot(L, cfg.max_iters)
+        s.set_params(cfg.tol, cfg.reg_strength)
+        s.load_image(c[1])
+        s.set_u0(None)
+        slots.append(s)
+    eng = engine.Engine(cuda, len(slots))
+    desc = engine.descriptors_to_device([s.desc for s in slots], cuda)
+    eng.commands(len(slots)).fill_(_lib.CMD_INIT)
+    finished_per_slice = []
+    for _ in range(10):
+        eng.run_slice(desc, len(slots), _lib.INTERP_CUBIC, 1 << 20, stop_flags=_lib.STOP_ON_FINISH)
+        torch.cuda.synchronize()
+        st = [int(s.info[1]) for s in slots]
+        finished_per_slice.append(sum(x != _lib.RUNNING for x in st))
+        if all(x != _lib.RUNNING for x in st):
+            break
+        eng.commands(len(slots)).fill_(_lib.CMD_RUN)
+    assert 1 <= finished_per_slice[0] < len(slots) and len(finished_per_slice) >= 2
+    assert finished_per_slice[-1] == len(slots)
+    for s, o in zip(slots, one):
+        assert int(s.info[0]) == o[1]
+        assert np.array_equal(s.u_out.cpu().numpy(), o[0])
