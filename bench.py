@@ -747,33 +747,37 @@ def run_adjoint(args, dev):
     adj.vjp(gu, rtol=1e-6)
     torch.cuda.synchronize()
     t_vjp = time.perf_counter() - t0
-    # one Hessian matvec pass (J^T J v + springs) over all R right-hand sides, timed alone with
-    # CUDA events on its stream; algorithmic bytes of the per-pixel form: 40 B per ROI pixel
-    # (image gradient 8 + node ids 16 + shape functions 16) + 16 B per node per right-hand side
-    from d2ic_gb300 import _lib
-    from d2ic_gb300._lib import ptr
-    Lh = adj.L
+    # one Hessian matvec pass (J^T J v + springs) over all R right-hand sides with the assembled
+    # node operator (the product the PCG runs), timed alone with CUDA events on its stream;
+    # algorithmic bytes of the per-pixel form: 40 B per ROI pixel (image gradient 8 + node ids 16 +
+    # shape functions 16) + 16 B per node per right-hand side; the kernel's own bytes: V read and Y
+    # written once (16 B per node per right-hand side) + the operator (320 B per node)
     V = torch.randn((wl.n_nodes, 2, R), generator=g, device=dev, dtype=torch.float32)
     Y = torch.empty_like(V)
-    slots = torch.zeros(Lh.node_chunk_k * Lh.n_nodes * 2 * R, dtype=torch.float32, device=dev)
     st = torch.cuda.current_stream()
+    adj.operator()
 
     def hv():
-        _lib.call("d2ic_hessian_matvec", ptr(adj.desc), Lh.n_chunks, Lh.n_nodes, ptr(adj.hess), ptr(V), R,
-                  adj.inv_np, adj.alpha, ptr(slots), ptr(Y), _lib.stream_handle())
+        adj.apply(V, Y)
     for _ in range(3):
         hv()
     reps = 20
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    times = []
     for _ in range(reps):
+        flush.fill_(1.0)                           # V, Y and the operator start outside L2
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
         hv()
-    e1.record(st)
-    torch.cuda.synchronize()
-    hv_ms = e0.elapsed_time(e1) / reps
+        e1.record(st)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    hv_ms = statistics.median(times)
     hv_bytes = 40 * wl.n_pix + 16 * R * wl.n_nodes
+    hv_own = 16 * R * wl.n_nodes + (16 * 16 + 16 * 4) * wl.n_nodes
     peak, peak_src = peaks()
     hv_rate = hv_bytes / (hv_ms * 1e-3) / 1e9
+    hv_own_rate = hv_own / (hv_ms * 1e-3) / 1e9
     # central finite differences of the exactly converged solution (Newton from u*)
     h = 1e-2
     D = args.adjoint_fd_dirs
@@ -796,11 +800,16 @@ def run_adjoint(args, dev):
             "u_std_px_median": float(u_std.median()), "strain_std_median": [float(v) for v in e_std.median(dim=0).values],
             "fd_directions": D, "fd_h": h, "fd_rel_err_max": max(rels) if rels else None,
             "fd_rel_err_median": statistics.median(rels) if rels else None, "fd_s": t_fd,
-            "hessian_matvec": {"rhs": R, "ms": hv_ms, "algorithmic_bytes": hv_bytes,
-                               "achieved_GBps": hv_rate, "peak_GBps": peak, "peak_source": peak_src,
-                               "frac": hv_rate / peak if peak else None,
-                               "note": "the kernel reads an exact 8x8 Hessian block per chunk instead of "
-                                       "per-pixel data, so it moves far fewer bytes than the per-pixel form"}}
+            "hessian_matvec": {"kernel": "hop_apply (assembled node operator)", "rhs": R, "ms": hv_ms,
+                               "algorithmic_bytes": hv_bytes, "achieved_GBps": hv_rate, "peak_GBps": peak,
+                               "peak_source": peak_src, "frac": hv_rate / peak if peak else None,
+                               "kernel_bytes": hv_own, "kernel_GBps": hv_own_rate,
+                               "kernel_frac": hv_own_rate / peak if peak else None,
+                               "l2": "flushed (256 MB write) before each timed launch",
+                               "note": "the Hessian is assembled once per linearisation point into per-node "
+                                       "2x2 blocks, so a product reads V and the operator and writes Y; "
+                                       "frac is against the per-pixel algorithmic bytes, kernel_frac "
+                                       "against the kernel's own bytes"}}
 
 
 # ---------------------------------------------------------------------------

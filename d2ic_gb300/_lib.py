@@ -89,6 +89,9 @@ _SIGS = {
     "d2ic_eval_objective": (i32, [vp, vp, vp, szt, i32, vp, vp, vp]),
     "d2ic_hessian_chunks": (i32, [vp, i32, vp, i32, vp, vp]),
     "d2ic_hessian_matvec": (i32, [vp, i32, i32, vp, vp, i32, f32, f32, vp, vp, vp]),
+    "d2ic_hessian_op_bytes": (szt, [i32, i32]),
+    "d2ic_hessian_assemble": (i32, [vp, i32, i32, i32, vp, f32, f32, vp, szt, vp]),
+    "d2ic_hessian_apply": (i32, [vp, i32, i32, vp, i32, vp, vp]),
     "d2ic_mixed_term": (i32, [vp, i32, i32, vp, vp, f32, vp, vp, i32, i32, vp]),
     "d2ic_mixed_term_batch": (i32, [vp, i32, i32, i32, vp, vp, i32, ctypes.c_longlong, f32, vp, vp, i32, i32, vp]),
     "d2ic_mixed_term_T": (i32, [vp, i32, vp, vp, f32, vp, vp]),

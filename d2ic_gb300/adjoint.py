@@ -76,8 +76,31 @@ class ImplicitAdjoint:
         self._active_u8 = self.active.to(torch.uint8).contiguous()
         self._pcg_work = None
 
+    def operator(self) -> torch.Tensor:
+        """The Hessian assembled into its node operator (d2ic_hessian_assemble), built once."""
+        if getattr(self, "_op", None) is None:
+            L = self.L
+            nb = int(_lib.load().d2ic_hessian_op_bytes(L.n_nodes, L.node_chunk_k))
+            self._op = torch.empty(nb, dtype=torch.uint8, device=self.dev)
+            _lib.call("d2ic_hessian_assemble", ptr(self.desc), L.n_chunks, L.n_nodes, L.node_chunk_k, ptr(self.hess),
+                      self.inv_np, self.alpha, ptr(self._op), nb, _lib.stream_handle())
+        return self._op
+
+    def apply(self, Vf: torch.Tensor, Y: torch.Tensor):
+        """Y = H Vf for float32 (Nn, 2, K) tensors with the assembled operator."""
+        L = self.L
+        _lib.call("d2ic_hessian_apply", ptr(self.operator()), L.n_nodes, L.node_chunk_k, ptr(Vf), int(Vf.shape[2]),
+                  ptr(Y), _lib.stream_handle())
+
     def matvec(self, V: torch.Tensor) -> torch.Tensor:
         """H V for V of shape (Nn, 2, K) (float64 in, float64 out; the kernels run in FP32)."""
+        Vf = V.to(torch.float32).contiguous()
+        Y = torch.empty_like(Vf)
+        self.apply(Vf, Y)
+        return Y.to(torch.float64)
+
+    def matvec_chunks(self, V: torch.Tensor) -> torch.Tensor:
+        """H V through the chunk blocks and node slots (d2ic_hessian_matvec, no assembly)."""
         L = self.L
         K = V.shape[2]
         Vf = V.to(torch.float32).contiguous()

@@ -1,14 +1,26 @@
-// Block-Jacobi preconditioned CG on the exact Hessian of the converged frame,
-// for K right-hand sides in lock step (the linear solves of the implicit
-// adjoint: H X = B).  Vectors are (n_nodes, 2, K) FP64 with the column index
-// fastest; H is applied in FP32 by d2ic_hessian_matvec; the 2x2 diagonal blocks'
-// inverses (Minv) and the active-dof mask come from the host.
+// The Hessian of the converged frame as an assembled node operator, and the
+// block-Jacobi preconditioned CG that solves H X = B for K right-hand sides in
+// lock step (the linear solves of the implicit adjoint).
 //
-// Per iteration: AP = H P (masked), pap = P.AP, a = rz / pap, X += a P,
-// R -= a AP, Z = Minv R, rr = R.R, rz' = R.Z, P = Z + (rz' / rz) P.  Every
-// column reduction is a per-block partial followed by a fixed-order sum over
-// blocks, so the solve is deterministic.  The host checks ||R|| <= rtol ||B||
-// for all columns after each iteration.
+// Assembly (once per linearisation point): the per-chunk element blocks
+// (d2ic_hessian_chunks: 10 symmetric 2x2 blocks per chunk) are scattered into
+// per-node slots (each chunk owns one slot of each of its nodes, so no atomics),
+// then one warp per node merges its slots and its springs into at most
+// D2IC_HOP_MAX (column node, symmetric 2x2 block) entries, in slot order:
+//     H_nj = (1/Np) sum_{chunks c at n, j} K^c_nj  +  alpha * springs.
+// Apply: Y = H V, one warp per node and 32 right-hand sides (lane = column),
+// V and Y laid out (node, component, k) with k fastest, so every neighbour read
+// is one coalesced 128-byte row; the entries of a node are read once for all
+// columns.  This replaces the chunk -> node-slot -> node pass per product (one
+// write and one read of node_chunk_k * Nn * 2 * K floats per product).
+//
+// PCG: per iteration three kernels -- AP = H P with the column sums P.AP fused,
+// the update of X, R, Z with the sums R.R and R.Z fused, the new direction --
+// each column sum a per-block partial reduced by the last block to finish, in
+// block order (deterministic).  The step kernel also decides convergence
+// (||R|| <= rtol ||B|| for every column) into a device flag that makes the later
+// kernels return at once, so the host launches iterations in batches and reads
+// the flag once per batch instead of synchronising every iteration.
 #include <stdlib.h>
 #include <string.h>
 
@@ -16,7 +28,201 @@
 
 namespace d2ic {
 
-constexpr int PT = 256;          // threads per block; thread t owns columns t, t + PT, ...
+constexpr int HOP = D2IC_HOP_MAX;   // operator entries per node
+static_assert(HOP <= 32, "one lane per operator entry");
+constexpr int PT = 256;             // threads per block of the node-range kernels
+
+__device__ __forceinline__ int hop_pair(int a, int b) {   // a <= b: index of the pair in 0..9
+    return a * 4 - (a * (a - 1)) / 2 + (b - a);
+}
+
+// operator storage inside the caller's buffer
+struct HopView {
+    float4 *blk;     // Nn * HOP: (xx, xy, yy, 0) of entry q of node n at n * HOP + q
+    int *idx;        // Nn * HOP: column node, -1 after the last entry
+    int *err;        // 1 int: set when a node has more than HOP distinct columns
+    int *sids;       // assembly scratch: node_chunk_k * Nn * 4 column nodes (-1: slot not owned)
+    float4 *sblk;    // node_chunk_k * Nn * 4 blocks
+};
+
+__host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+__host__ __device__ inline size_t hop_layout(int n_nodes, int node_chunk_k, char *base, HopView *v) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *p = base ? base + off : nullptr;
+        off += al256(bytes);
+        return p;
+    };
+    v->blk = (float4 *)take(sizeof(float4) * (size_t)n_nodes * HOP);
+    v->idx = (int *)take(sizeof(int) * (size_t)n_nodes * HOP);
+    v->err = (int *)take(sizeof(int));
+    v->sids = (int *)take(sizeof(int) * (size_t)node_chunk_k * n_nodes * 4);
+    v->sblk = (float4 *)take(sizeof(float4) * (size_t)node_chunk_k * n_nodes * 4);
+    return off;
+}
+
+// chunk pass: thread (c, a) writes row a of chunk c's element matrix into slot rank_a(c) of node n_a
+__global__ void __launch_bounds__(256) hop_scatter(const d2ic_frame_t *__restrict__ fp, const float *__restrict__ hess,
+                                                   int *__restrict__ sids, float4 *__restrict__ sblk) {
+    const d2ic_frame_t &F = *fp;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = t >> 2, a = t & 3;
+    if (c >= F.n_chunks) return;
+    const int n = __ldg(F.chunk_nodes + 4 * c + a);
+    const int s = (int)(((unsigned)__ldg(F.chunk_slot + c) >> (8 * a)) & 0xffu);
+    const size_t e = ((size_t)s * F.n_nodes + n) * 4;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int p = 3 * hop_pair(min(a, b), max(a, b));
+        sids[e + b] = __ldg(F.chunk_nodes + 4 * c + b);
+        sblk[e + b] = make_float4(__ldg(hess + 32 * (size_t)c + p), __ldg(hess + 32 * (size_t)c + p + 1),
+                                  __ldg(hess + 32 * (size_t)c + p + 2), 0.f);
+    }
+}
+
+// add (xx, xy, yy) to the entry of column j, appending it if new (whole warp; lane q holds entry q)
+__device__ __forceinline__ void hop_add(int &my_idx, float4 &my_blk, int &count, int &overflow, int j, float xx,
+                                        float xy, float yy, int lane) {
+    const unsigned hit = __ballot_sync(0xffffffffu, my_idx == j);
+    int q;
+    if (hit) {
+        q = __ffs(hit) - 1;
+    } else {
+        q = count;
+        if (q >= HOP) {
+            overflow = 1;
+            return;
+        }
+        ++count;
+        if (lane == q) my_idx = j;
+    }
+    if (lane == q) {
+        my_blk.x += xx;
+        my_blk.y += xy;
+        my_blk.z += yy;
+    }
+}
+
+// node pass: one warp per node merges its slots (slot order, row order) and its springs
+__global__ void __launch_bounds__(256) hop_merge(const d2ic_frame_t *__restrict__ fp, const int *__restrict__ sids,
+                                                 const float4 *__restrict__ sblk, float inv_np, float alpha,
+                                                 int *__restrict__ idx, float4 *__restrict__ blk, int *__restrict__ err) {
+    const d2ic_frame_t &F = *fp;
+    const int lane = threadIdx.x & 31;
+    const int n = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (n >= F.n_nodes) return;
+    const size_t Nn = F.n_nodes;
+    int my_idx = -1, count = 0, overflow = 0;
+    float4 my_blk = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int s = 0; s < F.node_chunk_k; ++s) {
+        const size_t e = ((size_t)s * Nn + n) * 4;
+        const int jl = lane < 4 ? __ldg(sids + e + lane) : -1;
+        const float4 bl = lane < 4 ? __ldg(sblk + e + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int b = 0; b < 4; ++b) {
+            const int j = __shfl_sync(0xffffffffu, jl, b);
+            if (j < 0) break;   // slot not owned by a chunk (uniform)
+            hop_add(my_idx, my_blk, count, overflow, j, inv_np * __shfl_sync(0xffffffffu, bl.x, b),
+                    inv_np * __shfl_sync(0xffffffffu, bl.y, b), inv_np * __shfl_sync(0xffffffffu, bl.z, b), lane);
+        }
+    }
+    for (int q = 0; q < F.max_deg; ++q) {                 // springs: alpha * w on the diagonal, -alpha * w off it
+        const int j = __ldg(F.nbr_index + (size_t)q * Nn + n);
+        if (j < 0) break;
+        const float w = alpha * __ldg(F.nbr_weight + (size_t)q * Nn + n);
+        hop_add(my_idx, my_blk, count, overflow, n, w, 0.f, w, lane);
+        hop_add(my_idx, my_blk, count, overflow, j, -w, 0.f, -w, lane);
+    }
+    if (lane < HOP) {
+        idx[(size_t)n * HOP + lane] = my_idx;
+        blk[(size_t)n * HOP + lane] = my_blk;
+    }
+    if (overflow && lane == 0) atomicExch(err, 1);
+}
+
+// one node (warp) x 32 columns (lanes): y = sum_q blk_q v_{idx_q}
+__device__ __forceinline__ void hop_row(const int *__restrict__ idx, const float4 *__restrict__ blk, int n, int K, int k,
+                                        const float *__restrict__ V, int lane, float &yx, float &yy) {
+    const int my_idx = lane < HOP ? __ldg(idx + (size_t)n * HOP + lane) : -1;
+    const float4 my_blk = lane < HOP ? __ldg(blk + (size_t)n * HOP + lane) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned live = __ballot_sync(0xffffffffu, my_idx >= 0);
+    const int cnt = __popc(live);                          // entries are packed from lane 0
+    yx = 0.f;
+    yy = 0.f;
+    constexpr int UB = 8;
+    for (int q0 = 0; q0 < cnt; q0 += UB) {
+        float vx[UB], vy[UB];
+        int jj[UB];
+#pragma unroll
+        for (int u = 0; u < UB; ++u) {
+            jj[u] = __shfl_sync(0xffffffffu, my_idx, (q0 + u) & 31);
+            const bool ok = q0 + u < cnt && k < K;
+            vx[u] = ok ? __ldg(V + ((size_t)jj[u] * 2) * K + k) : 0.f;
+            vy[u] = ok ? __ldg(V + ((size_t)jj[u] * 2 + 1) * K + k) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < UB; ++u) {
+            const int q = (q0 + u) & 31;
+            const float bx = __shfl_sync(0xffffffffu, my_blk.x, q), by = __shfl_sync(0xffffffffu, my_blk.y, q),
+                        bz = __shfl_sync(0xffffffffu, my_blk.z, q);
+            if (q0 + u < cnt) {
+                yx = __fmaf_rn(bx, vx[u], __fmaf_rn(by, vy[u], yx));
+                yy = __fmaf_rn(by, vx[u], __fmaf_rn(bz, vy[u], yy));
+            }
+        }
+    }
+}
+
+// Y = H V: block = 8 nodes (warps) x 32 columns
+__global__ void __launch_bounds__(256) hop_apply(const int *__restrict__ idx, const float4 *__restrict__ blk,
+                                                 int n_nodes, const float *__restrict__ V, int K, float *__restrict__ Y) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n = blockIdx.x * 8 + w, k = blockIdx.y * 32 + lane;
+    if (n >= n_nodes) return;
+    float yx, yy;
+    hop_row(idx, blk, n, K, k, V, lane, yx, yy);
+    if (k < K) {
+        Y[((size_t)n * 2) * K + k] = yx;
+        Y[((size_t)n * 2 + 1) * K + k] = yy;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// PCG
+// ---------------------------------------------------------------------------
+struct PcgCtl {
+    int done;        // all columns converged: later kernels return at once
+    int iters;       // iterations whose update ran
+    int cnt_step;    // last-block counters (reset by the last block)
+    int cnt_init;
+    int cnt_pap[1];  // one per 32-column tile (variable length, at the end)
+};
+
+__device__ __forceinline__ int ld_flag(const int *p) { return *(volatile const int *)p; }
+
+// the last block to arrive (after writing its partials) returns true; the counter is reset
+__device__ __forceinline__ bool last_block(int *cnt, int nblocks) {
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int t = atomicAdd(cnt, 1);
+        s_last = t == nblocks - 1;
+        if (s_last) *cnt = 0;
+    }
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last;
+}
+
+// out[k] = sum over blocks b (in order) of part[b * K + k], whole block, columns k0 .. k1-1
+__device__ void reduce_cols(const double *part, int nb, int K, int k0, int k1, double *out) {
+    for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nb; ++b) s += __ldcg(part + (size_t)b * K + k);
+        out[k] = s;
+    }
+}
 
 // nodes [n0, n1) of block b
 __device__ __forceinline__ void node_range(int n_nodes, int &n0, int &n1) {
@@ -29,11 +235,12 @@ __global__ void __launch_bounds__(PT) pcg_init(int n_nodes, int K, const double 
                                                const unsigned char *__restrict__ act, const double *__restrict__ Minv,
                                                double *__restrict__ X, double *__restrict__ R, double *__restrict__ Z,
                                                double *__restrict__ P, float *__restrict__ Pf,
-                                               double *__restrict__ part_rz, double *__restrict__ part_bb) {
+                                               double *__restrict__ part_rz, double *__restrict__ part_bb,
+                                               double *__restrict__ rz, double *__restrict__ bb, PcgCtl *ctl) {
     int n0, n1;
     node_range(n_nodes, n0, n1);
     for (int k = threadIdx.x; k < K; k += PT) {
-        double rz = 0.0, bb = 0.0;
+        double srz = 0.0, sbb = 0.0;
         for (int n = n0; n < n1; ++n) {
             const double m = act[n] ? 1.0 : 0.0;
             const size_t i0 = ((size_t)n * 2) * K + k, i1 = i0 + K;
@@ -50,26 +257,50 @@ __global__ void __launch_bounds__(PT) pcg_init(int n_nodes, int K, const double 
             P[i1] = z1;
             Pf[i0] = (float)z0;
             Pf[i1] = (float)z1;
-            rz += b0 * z0 + b1 * z1;
-            bb += b0 * b0 + b1 * b1;
+            srz += b0 * z0 + b1 * z1;
+            sbb += b0 * b0 + b1 * b1;
         }
-        part_rz[(size_t)blockIdx.x * K + k] = rz;
-        part_bb[(size_t)blockIdx.x * K + k] = bb;
+        part_rz[(size_t)blockIdx.x * K + k] = srz;
+        part_bb[(size_t)blockIdx.x * K + k] = sbb;
+    }
+    if (last_block(&ctl->cnt_init, gridDim.x)) {
+        reduce_cols(part_rz, gridDim.x, K, 0, K, rz);
+        reduce_cols(part_bb, gridDim.x, K, 0, K, bb);
     }
 }
 
-__global__ void __launch_bounds__(PT) pcg_pap(int n_nodes, int K, const double *__restrict__ P, const float *__restrict__ AP,
-                                              const unsigned char *__restrict__ act, double *__restrict__ part) {
-    int n0, n1;
-    node_range(n_nodes, n0, n1);
-    for (int k = threadIdx.x; k < K; k += PT) {
-        double s = 0.0;
-        for (int n = n0; n < n1; ++n) {
-            if (!act[n]) continue;
+// AP = H P (masked to active dofs) and pap[k] = P.AP: block = 8 nodes x 32 columns
+__global__ void __launch_bounds__(256) pcg_apply(const int *__restrict__ idx, const float4 *__restrict__ blk,
+                                                 int n_nodes, int K, const float *__restrict__ Pf,
+                                                 const double *__restrict__ P, const unsigned char *__restrict__ act,
+                                                 float *__restrict__ AP, double *__restrict__ part,
+                                                 double *__restrict__ pap, PcgCtl *ctl) {
+    if (ld_flag(&ctl->done)) return;
+    __shared__ double s_p[8][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n = blockIdx.x * 8 + w, k = blockIdx.y * 32 + lane;
+    double pp = 0.0;
+    if (n < n_nodes) {
+        float yx, yy;
+        hop_row(idx, blk, n, K, k, Pf, lane, yx, yy);
+        if (k < K) {
             const size_t i0 = ((size_t)n * 2) * K + k, i1 = i0 + K;
-            s += P[i0] * (double)AP[i0] + P[i1] * (double)AP[i1];
+            AP[i0] = yx;
+            AP[i1] = yy;
+            if (act[n]) pp = P[i0] * (double)yx + P[i1] * (double)yy;
         }
-        part[(size_t)blockIdx.x * K + k] = s;
+    }
+    s_p[w][lane] = pp;
+    __syncthreads();
+    if (w == 0) {
+        double s = 0.0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) s += s_p[i][lane];
+        if (k < K) part[(size_t)blockIdx.x * K + k] = s;
+    }
+    if (last_block(&ctl->cnt_pap[blockIdx.y], gridDim.x)) {
+        const int k0 = blockIdx.y * 32, k1 = min(k0 + 32, K);
+        reduce_cols(part, gridDim.x, K, k0, k1, pap);
     }
 }
 
@@ -78,12 +309,15 @@ __global__ void __launch_bounds__(PT) pcg_step(int n_nodes, int K, const double 
                                                const double *__restrict__ Minv, double *__restrict__ X,
                                                double *__restrict__ R, double *__restrict__ Z,
                                                const double *__restrict__ P, const float *__restrict__ AP,
-                                               double *__restrict__ part_rr, double *__restrict__ part_rz) {
+                                               double *__restrict__ part_rr, double *__restrict__ part_rz,
+                                               double *__restrict__ rr, double *__restrict__ rz_new,
+                                               const double *__restrict__ bb, double rtol, PcgCtl *ctl) {
+    if (ld_flag(&ctl->done)) return;
     int n0, n1;
     node_range(n_nodes, n0, n1);
     for (int k = threadIdx.x; k < K; k += PT) {
         const double a = pap[k] > 0.0 ? rz[k] / pap[k] : 0.0;
-        double rr = 0.0, rzn = 0.0;
+        double srr = 0.0, srz = 0.0;
         for (int n = n0; n < n1; ++n) {
             const double m = act[n] ? 1.0 : 0.0;
             const size_t i0 = ((size_t)n * 2) * K + k, i1 = i0 + K;
@@ -96,17 +330,33 @@ __global__ void __launch_bounds__(PT) pcg_step(int n_nodes, int K, const double 
             const double z0 = M[0] * r0 + M[1] * r1, z1 = M[2] * r0 + M[3] * r1;
             Z[i0] = z0;
             Z[i1] = z1;
-            rr += r0 * r0 + r1 * r1;
-            rzn += r0 * z0 + r1 * z1;
+            srr += r0 * r0 + r1 * r1;
+            srz += r0 * z0 + r1 * z1;
         }
-        part_rr[(size_t)blockIdx.x * K + k] = rr;
-        part_rz[(size_t)blockIdx.x * K + k] = rzn;
+        part_rr[(size_t)blockIdx.x * K + k] = srr;
+        part_rz[(size_t)blockIdx.x * K + k] = srz;
+    }
+    if (last_block(&ctl->cnt_step, gridDim.x)) {
+        reduce_cols(part_rr, gridDim.x, K, 0, K, rr);
+        reduce_cols(part_rz, gridDim.x, K, 0, K, rz_new);
+        __syncthreads();
+        int ok = 1;
+        for (int k = threadIdx.x; k < K; k += PT) {
+            const double bn = fmax(sqrt(__ldcg(bb + k)), 1e-300);
+            ok &= sqrt(__ldcg(rr + k)) <= rtol * bn;
+        }
+        ok = __syncthreads_and(ok);
+        if (threadIdx.x == 0) {
+            ctl->iters += 1;
+            if (ok) ctl->done = 1;
+        }
     }
 }
 
 __global__ void __launch_bounds__(PT) pcg_dir(int n_nodes, int K, const double *__restrict__ rz_old,
                                               const double *__restrict__ rz_new, const double *__restrict__ Z,
-                                              double *__restrict__ P, float *__restrict__ Pf) {
+                                              double *__restrict__ P, float *__restrict__ Pf, const PcgCtl *ctl) {
+    if (ld_flag(&ctl->done)) return;
     int n0, n1;
     node_range(n_nodes, n0, n1);
     for (int k = threadIdx.x; k < K; k += PT) {
@@ -122,28 +372,26 @@ __global__ void __launch_bounds__(PT) pcg_dir(int n_nodes, int K, const double *
     }
 }
 
-// out[k] = sum over blocks of part[b][k]: one warp per column, lane l sums blocks l, l + 32, ...
-// in order, then a fixed shuffle tree (deterministic)
-__global__ void pcg_reduce(int nb, int K, const double *__restrict__ part, double *__restrict__ out) {
-    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (k >= K) return;
-    double s = 0.0;
-    for (int b = lane; b < nb; b += 32) s += part[(size_t)b * K + k];
-    s = warp_sum_d(s);
-    if (lane == 0) out[k] = s;
-}
-
 struct PcgWork {
     double *R, *Z, *P, *part_a, *part_b, *rz, *rz2, *pap, *rr, *bb;
-    float *Pf, *AP, *slots;
+    float *Pf, *AP;
+    PcgCtl *ctl;
+    char *op;
 };
 
-static size_t carve(int n_nodes, int K, int node_chunk_k, int nb, char *base, PcgWork *w) {
+static int pcg_blocks(int n_nodes) {
+    int nb = (n_nodes + 15) / 16;                 // >= 16 nodes per block
+    return nb < 1 ? 1 : (nb > 1024 ? 1024 : nb);
+}
+
+static size_t carve(int n_nodes, int K, int node_chunk_k, char *base, PcgWork *w) {
     const size_t v = (size_t)n_nodes * 2 * K;
+    const int nb = pcg_blocks(n_nodes), na = (n_nodes + 7) / 8;
+    const int nparts = nb > na ? nb : na;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         char *p = base ? base + off : nullptr;
-        off += (bytes + 255) & ~(size_t)255;
+        off += al256(bytes);
         return p;
     };
     w->R = (double *)take(sizeof(double) * v);
@@ -151,32 +399,87 @@ static size_t carve(int n_nodes, int K, int node_chunk_k, int nb, char *base, Pc
     w->P = (double *)take(sizeof(double) * v);
     w->Pf = (float *)take(sizeof(float) * v);
     w->AP = (float *)take(sizeof(float) * v);
-    w->slots = (float *)take(sizeof(float) * (size_t)node_chunk_k * v);
-    w->part_a = (double *)take(sizeof(double) * (size_t)nb * K);
-    w->part_b = (double *)take(sizeof(double) * (size_t)nb * K);
+    w->part_a = (double *)take(sizeof(double) * (size_t)nparts * K);
+    w->part_b = (double *)take(sizeof(double) * (size_t)nparts * K);
     w->rz = (double *)take(sizeof(double) * K);
     w->rz2 = (double *)take(sizeof(double) * K);
     w->pap = (double *)take(sizeof(double) * K);
     w->rr = (double *)take(sizeof(double) * K);
     w->bb = (double *)take(sizeof(double) * K);
+    w->ctl = (PcgCtl *)take(sizeof(PcgCtl) + sizeof(int) * (size_t)((K + 31) / 32));
+    HopView hv;
+    w->op = take(hop_layout(n_nodes, node_chunk_k, nullptr, &hv));
     return off;
 }
 
-static int pcg_blocks(int n_nodes) {
-    int nb = (n_nodes + 15) / 16;                 // >= 16 nodes per block
-    return nb < 1 ? 1 : (nb > 1024 ? 1024 : nb);
+static int assemble(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
+                    const float *chunk_hess, float inv_np, float alpha_reg, char *op, cudaStream_t s, HopView *hv) {
+    hop_layout(n_nodes, node_chunk_k, op, hv);
+    cudaError_t e = cudaMemsetAsync(hv->sids, 0xff, sizeof(int) * (size_t)node_chunk_k * n_nodes * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(hv->err, 0, sizeof(int), s);
+    if (e != cudaSuccess) return cuda_status(e, "hessian assembly scratch");
+    if (n_chunks > 0) {
+        hop_scatter<<<(unsigned)((4 * (size_t)n_chunks + 255) / 256), 256, 0, s>>>(frame_dev, chunk_hess, hv->sids,
+                                                                                 hv->sblk);
+        D2IC_CHECK_LAUNCH("hop_scatter");
+    }
+    hop_merge<<<(unsigned)((32 * (size_t)n_nodes + 255) / 256), 256, 0, s>>>(frame_dev, hv->sids, hv->sblk, inv_np,
+                                                                           alpha_reg, hv->idx, hv->blk, hv->err);
+    D2IC_CHECK_LAUNCH("hop_merge");
+    return D2IC_OK;
+}
+
+static int check_overflow(const HopView &hv, cudaStream_t s) {
+    int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, hv.err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "hessian assembly");
+    D2IC_REQUIRE(err == 0, "hessian assembly: a node couples to more than %d nodes", HOP);
+    return D2IC_OK;
 }
 
 }  // namespace d2ic
 
 using namespace d2ic;
 
+extern "C" size_t d2ic_hessian_op_bytes(int n_nodes, int node_chunk_k) {
+    HopView hv;
+    if (n_nodes < 1) n_nodes = 1;
+    if (node_chunk_k < 1) node_chunk_k = 1;
+    return hop_layout(n_nodes, node_chunk_k, nullptr, &hv);
+}
+
+extern "C" int d2ic_hessian_assemble(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
+                                     const float *chunk_hess, float inv_np, float alpha_reg, void *op, size_t op_bytes,
+                                     void *stream) {
+    D2IC_REQUIRE(frame_dev && op && (chunk_hess || n_chunks == 0) && n_nodes >= 1 && node_chunk_k >= 1 && n_chunks >= 0,
+                 "d2ic_hessian_assemble: bad arguments");
+    D2IC_REQUIRE(((uintptr_t)op & 255) == 0, "d2ic_hessian_assemble: op must be 256-byte aligned");
+    D2IC_REQUIRE(op_bytes >= d2ic_hessian_op_bytes(n_nodes, node_chunk_k), "d2ic_hessian_assemble: op buffer too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    HopView hv;
+    int st = assemble(frame_dev, n_chunks, n_nodes, node_chunk_k, chunk_hess, inv_np, alpha_reg, (char *)op, s, &hv);
+    if (st) return st;
+    return check_overflow(hv, s);
+}
+
+extern "C" int d2ic_hessian_apply(const void *op, int n_nodes, int node_chunk_k, const float *V, int K, float *Y,
+                                  void *stream) {
+    D2IC_REQUIRE(op && V && Y && n_nodes >= 1 && K >= 1 && node_chunk_k >= 1, "d2ic_hessian_apply: bad arguments");
+    HopView hv;
+    hop_layout(n_nodes, node_chunk_k, (char *)op, &hv);
+    hop_apply<<<dim3((unsigned)((n_nodes + 7) / 8), (unsigned)((K + 31) / 32)), 256, 0, (cudaStream_t)stream>>>(
+        hv.idx, hv.blk, n_nodes, V, K, Y);
+    D2IC_CHECK_LAUNCH("hop_apply");
+    return D2IC_OK;
+}
+
 extern "C" size_t d2ic_pcg_work_bytes(int n_nodes, int K, int node_chunk_k) {
     PcgWork w;
     if (n_nodes < 1) n_nodes = 1;
     if (K < 1) K = 1;
     if (node_chunk_k < 1) node_chunk_k = 1;
-    return carve(n_nodes, K, node_chunk_k, pcg_blocks(n_nodes), nullptr, &w);
+    return carve(n_nodes, K, node_chunk_k, nullptr, &w);
 }
 
 extern "C" int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
@@ -187,64 +490,45 @@ extern "C" int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n
                      node_chunk_k >= 1 && max_iter >= 0,
                  "d2ic_pcg_solve: bad arguments");
     D2IC_REQUIRE(((uintptr_t)work & 255) == 0, "d2ic_pcg_solve: work must be 256-byte aligned");
-    const int nb = pcg_blocks(n_nodes);
     PcgWork w;
-    const size_t need = carve(n_nodes, K, node_chunk_k, nb, (char *)work, &w);
+    const size_t need = carve(n_nodes, K, node_chunk_k, (char *)work, &w);
     D2IC_REQUIRE(work_bytes >= need, "d2ic_pcg_solve: work %zu bytes < %zu needed", work_bytes, need);
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t v = (size_t)n_nodes * 2 * K;
-    // slots that no chunk owns must read as 0; owned ones are rewritten by every matvec
-    cudaError_t e = cudaMemsetAsync(w.slots, 0, sizeof(float) * (size_t)node_chunk_k * v, s);
-    if (e != cudaSuccess) return cuda_status(e, "pcg slots");
-    const int rb = (K + 7) / 8;                    // pcg_reduce: 8 warps (columns) per block
-    pcg_init<<<nb, PT, 0, s>>>(n_nodes, K, B, active, Minv, X, w.R, w.Z, w.P, w.Pf, w.part_a, w.part_b);
-    pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_a, w.rz);
-    pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_b, w.bb);
-    D2IC_CHECK_LAUNCH("pcg init");
-    double *host = (double *)malloc(sizeof(double) * 2 * K);
-    if (!host) {
-        set_error("d2ic_pcg_solve: host allocation failed");
-        return D2IC_OOM;
-    }
-    double *h_rr = host, *h_bb = host + K;
-    e = cudaMemcpyAsync(h_bb, w.bb, sizeof(double) * K, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        free(host);
-        return cuda_status(e, "pcg norms");
-    }
-    int it = 0, st = D2IC_OK;
-    double *rz = w.rz, *rz_new = w.rz2;
-    for (it = 1; it <= max_iter; ++it) {
-        st = d2ic_hessian_matvec(frame_dev, n_chunks, n_nodes, chunk_hess, w.Pf, K, inv_np, alpha_reg, w.slots, w.AP,
-                                 stream);
-        if (st) break;
-        pcg_pap<<<nb, PT, 0, s>>>(n_nodes, K, w.P, w.AP, active, w.part_a);
-        pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_a, w.pap);
-        pcg_step<<<nb, PT, 0, s>>>(n_nodes, K, rz, w.pap, active, Minv, X, w.R, w.Z, w.P, w.AP, w.part_a, w.part_b);
-        pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_a, w.rr);
-        pcg_reduce<<<rb, 256, 0, s>>>(nb, K, w.part_b, rz_new);
-        e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaMemcpyAsync(h_rr, w.rr, sizeof(double) * K, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) {
-            st = cuda_status(e, "pcg iteration");
-            break;
-        }
-        bool done = true;
-        for (int k = 0; k < K && done; ++k) {
-            const double bn = sqrt(h_bb[k]) > 1e-300 ? sqrt(h_bb[k]) : 1e-300;
-            done = sqrt(h_rr[k]) <= rtol * bn;
-        }
-        if (done) break;
-        pcg_dir<<<nb, PT, 0, s>>>(n_nodes, K, rz, rz_new, w.Z, w.P, w.Pf);
-        double *t = rz;
-        rz = rz_new;
-        rz_new = t;
-    }
-    free(host);
-    if (iters_out) *iters_out = it > max_iter ? max_iter : it;
+    HopView hv;
+    int st = assemble(frame_dev, n_chunks, n_nodes, node_chunk_k, chunk_hess, inv_np, alpha_reg, w.op, s, &hv);
     if (st) return st;
-    D2IC_CHECK_LAUNCH("pcg loop");
+    const size_t ctl_bytes = sizeof(PcgCtl) + sizeof(int) * (size_t)((K + 31) / 32);
+    cudaError_t e = cudaMemsetAsync(w.ctl, 0, ctl_bytes, s);
+    if (e != cudaSuccess) return cuda_status(e, "pcg control");
+    const int nb = pcg_blocks(n_nodes);
+    pcg_init<<<nb, PT, 0, s>>>(n_nodes, K, B, active, Minv, X, w.R, w.Z, w.P, w.Pf, w.part_a, w.part_b, w.rz, w.bb,
+                               w.ctl);
+    D2IC_CHECK_LAUNCH("pcg init");
+    st = check_overflow(hv, s);                      // also waits for the assembly
+    if (st) return st;
+    const dim3 ag((unsigned)((n_nodes + 7) / 8), (unsigned)((K + 31) / 32));
+    constexpr int BATCH = 8;                         // iterations launched per host check of the flag
+    int it = 0;
+    PcgCtl host_ctl = {};
+    double *rz = w.rz, *rz_new = w.rz2;
+    while (it < max_iter) {
+        const int nb_it = max_iter - it < BATCH ? max_iter - it : BATCH;
+        for (int i = 0; i < nb_it; ++i) {
+            pcg_apply<<<ag, 256, 0, s>>>(hv.idx, hv.blk, n_nodes, K, w.Pf, w.P, active, w.AP, w.part_a, w.pap, w.ctl);
+            pcg_step<<<nb, PT, 0, s>>>(n_nodes, K, rz, w.pap, active, Minv, X, w.R, w.Z, w.P, w.AP, w.part_a,
+                                       w.part_b, w.rr, rz_new, w.bb, rtol, w.ctl);
+            pcg_dir<<<nb, PT, 0, s>>>(n_nodes, K, rz, rz_new, w.Z, w.P, w.Pf, w.ctl);
+            double *t = rz;
+            rz = rz_new;
+            rz_new = t;
+        }
+        it += nb_it;
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&host_ctl, w.ctl, sizeof(PcgCtl), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_status(e, "pcg iteration");
+        if (host_ctl.done) break;
+    }
+    if (iters_out) *iters_out = host_ctl.iters;
     return D2IC_OK;
 }

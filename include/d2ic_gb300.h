@@ -166,10 +166,11 @@ D2IC_API int d2ic_pack_pixels(const int *colrow, const float *xieta, int n,
 /* Bytes of device scratch d2ic_pcg_solve needs (256-byte aligned base). */
 D2IC_API size_t d2ic_pcg_work_bytes(int n_nodes, int K, int node_chunk_k);
 
-/* X = H^-1 B for B, X (n_nodes, 2, K) FP64 (column index fastest), H applied by
- * d2ic_hessian_matvec from chunk_hess, Minv (n_nodes, 2, 2) FP64 inverse diagonal
- * blocks (zero for inactive dofs), active (n_nodes) 0/1 mask.  Stops when every
- * column has ||R|| <= rtol ||B|| or after max_iter iterations (*iters_out). */
+/* X = H^-1 B for B, X (n_nodes, 2, K) FP64 (column index fastest), H assembled from chunk_hess
+ * into the work buffer (as d2ic_hessian_assemble) and applied in FP32, Minv (n_nodes, 2, 2) FP64
+ * inverse diagonal blocks (zero for inactive dofs), active (n_nodes) 0/1 mask.  Stops when every
+ * column has ||R|| <= rtol ||B|| or after max_iter iterations (*iters_out); convergence is decided
+ * on the device and read by the host once per batch of 8 iterations. */
 D2IC_API int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
                             const float *chunk_hess, float inv_np, float alpha_reg, const double *Minv,
                             const unsigned char *active, const double *B, double *X, int K, double rtol,
@@ -336,6 +337,20 @@ D2IC_API int d2ic_hessian_chunks(const d2ic_frame_t *frame_dev, int n_chunks, co
 D2IC_API int d2ic_hessian_matvec(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, const float *chunk_hess,
                                  const float *V, int K, float inv_np, float alpha_reg, float *slots, float *Y,
                                  void *stream);
+/* The same operator assembled once per linearisation point: per node at most D2IC_HOP_MAX
+ * (column node, symmetric 2x2 block) entries, chunk blocks / Np plus alpha_reg times the spring
+ * Hessian, merged in slot order (no atomics).  op: device buffer of d2ic_hessian_op_bytes(), 256-byte
+ * aligned.  Returns D2IC_BAD_ARG if a node couples to more than D2IC_HOP_MAX nodes (a Q4 grid node
+ * couples to at most 9). */
+#define D2IC_HOP_MAX 16
+D2IC_API size_t d2ic_hessian_op_bytes(int n_nodes, int node_chunk_k);
+D2IC_API int d2ic_hessian_assemble(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, int node_chunk_k,
+                                   const float *chunk_hess, float inv_np, float alpha_reg, void *op, size_t op_bytes,
+                                   void *stream);
+/* Y = H V with the assembled operator, V and Y (n_nodes, 2, K), K fastest: one coalesced row of V per
+ * neighbour and 32 columns, no scratch. */
+D2IC_API int d2ic_hessian_apply(const void *op, int n_nodes, int node_chunk_k, const float *V, int K, float *Y,
+                                void *stream);
 /* Column k of out (n_nodes x 2 x K) = scale * (d grad_u J / dI2) dI, dI given by its
  * B-spline coefficients (halo layout of the frame).  slots: node_chunk_k * n_nodes * 2 floats. */
 D2IC_API int d2ic_mixed_term(const d2ic_frame_t *frame_dev, int n_chunks, int n_nodes, const float *u,

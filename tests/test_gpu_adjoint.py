@@ -110,3 +110,18 @@ def test_strain_jvp_matches_finite_difference(problem):
     Ep = ostrain.to_voigt(ostrain.green_lagrange_nodes_lsq(u + h * du, X, idx, deg, 8.0)[1])
     Em = ostrain.to_voigt(ostrain.green_lagrange_nodes_lsq(u - h * du, X, idx, deg, 8.0)[1])
     assert np.abs(d - (Ep - Em) / (2 * h)).max() <= 1e-8
+
+
+@pytest.mark.parametrize("K", [1, 37, 256])
+def test_assembled_operator_equals_chunk_matvec(problem, K):
+    """The assembled node operator (d2ic_hessian_assemble / d2ic_hessian_apply) applies the same
+    Hessian as the chunk-block product through node slots (d2ic_hessian_matvec), to FP32 rounding."""
+    adj = _adj(problem)
+    Nn = problem["u"].shape[0]
+    g = torch.Generator(device=problem["u"].device).manual_seed(7)
+    V = torch.randn((Nn, 2, K), generator=g, device=problem["u"].device, dtype=torch.float64)
+    V[~adj.active] = 0.0
+    a = adj.matvec(V)
+    b = adj.matvec_chunks(V)
+    scale = float(b.abs().max())
+    assert float((a - b).abs().max()) <= 1e-5 * scale
