@@ -61,6 +61,15 @@ class Frame(ctypes.Structure):
     ]
 
 
+class Grid(ctypes.Structure):
+    """d2ic_grid_t: a tensor-grid mesh and ROI mask on the device (include/d2ic_gb300.h)."""
+    _fields_ = [
+        ("gx", vp), ("gy", vp), ("nx", i32), ("ny", i32), ("cell", vp), ("elem_cell", vp), ("elements", vp),
+        ("nodes", vp), ("roi", vp), ("n_elem", i32), ("n_nodes", i32), ("H", i32), ("W", i32),
+        ("i0", i32), ("i1", i32), ("j0", i32), ("j1", i32),
+    ]
+
+
 _SIGS = {
     "d2ic_last_error_string": (ctypes.c_char_p, []),
     "d2ic_version": (i32, []),
@@ -102,6 +111,11 @@ _SIGS = {
     "d2ic_discrepancy_map": (i32, [vp, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),
     "d2ic_central_gradient": (i32, [vp, i32, i32, vp, vp, vp]),
     "d2ic_local_coordinates": (i32, [vp, vp, vp, ctypes.c_longlong, i32, vp, vp, vp]),
+    "d2ic_grid_count": (i32, [vp, vp, vp]),
+    "d2ic_grid_scratch_bytes": (szt, [ctypes.c_longlong, i32]),
+    "d2ic_grid_layout": (i32, [vp, vp, vp, ctypes.c_longlong, i32, i32, vp, i32, i32, vp, szt, vp, vp, vp, vp, vp, vp,
+                               vp, vp]),
+    "d2ic_grid_springs": (i32, [vp, vp, i32, vp, vp, vp]),
     "d2ic_structured_assign": (i32, [vp, ctypes.c_longlong, vp, i32, vp, i32, vp, vp, vp]),
     "d2ic_pcg_work_bytes": (szt, [i32, i32, i32]),
     "d2ic_pcg_solve": (i32, [vp, i32, i32, i32, vp, f32, f32, vp, vp, vp, vp, i32, f64, i32, vp, szt, vp, vp]),

@@ -40,18 +40,39 @@ class LaunchShape:
     us_per_round: float = float("nan")
 
 
-def frame_signature(pix, H: int, W: int, interpolation: str) -> str:
-    """Key of frames that share a launch shape: size, ROI pixels (to 1/64), element size."""
+def _element_pixels(pix):
+    """Pixels per element of a frame's assets (zeros dropped)."""
     from .engine import _elements_of
-    n_pix = int(np.asarray(pix.pixel_coords_ref).shape[0])
-    elem = 0
-    if n_pix:
-        # the most common pixels-per-element count (interior elements), as an element-size estimate
+    if hasattr(type(pix), "element_pixel_counts"):           # GridPixelData: counted on the device
+        per_elem = np.asarray(pix.element_pixel_counts())
+    else:
+        if int(np.asarray(pix.pixel_coords_ref).shape[0]) == 0:
+            return np.zeros(0, np.int64)
         per_elem = np.bincount(_elements_of(pix))
-        counts = np.bincount(per_elem[per_elem > 0])
-        elem = int(round(np.sqrt(int(np.argmax(counts)))))
-    bucket = int(round(64 * np.log2(max(n_pix, 1))))
+    return per_elem[per_elem > 0]
+
+
+def frame_signature(pix, H: int, W: int, interpolation: str) -> str:
+    """Key of frames that share a launch shape: size, element size, ROI pixels to within a factor
+    of 2^(1/4) (ROI coverage moves the best shape little; finer keys re-tune nearly every frame)."""
+    pe = _element_pixels(pix)
+    n_pix = int(pe.sum())
+    elem = 0
+    if pe.size:
+        # the most common pixels-per-element count (interior elements), as an element-size estimate
+        elem = int(round(np.sqrt(int(np.argmax(np.bincount(pe))))))
+    bucket = int(round(4 * np.log2(max(n_pix, 1))))
     return f"{H}x{W}:{interpolation}:e{elem}:p{bucket}"
+
+
+def distinct_chunk_sizes(candidates, max_element_pixels: int):
+    """Chunk sizes that give different layouts: a chunk holds pixels of one element, so every
+    size at or above the largest element's pixel count gives the same chunks; keep the smallest."""
+    out = sorted(c for c in candidates if c < max_element_pixels)
+    big = [c for c in candidates if c >= max_element_pixels]
+    if big:
+        out.append(min(big))
+    return tuple(out)
 
 
 def device_blocks(device) -> int:
@@ -112,7 +133,8 @@ class Autotuner:
         grids = sorted({max(1, int(round(full * f))) for f in self.grid_fractions}, reverse=True)
         eng = Engine(self.device, 1)
         trials = []
-        for chunk in self.chunk_candidates:
+        pe = _element_pixels(pix)
+        for chunk in distinct_chunk_sizes(self.chunk_candidates, int(pe.max()) if pe.size else 1):
             layout = FrameLayout(pix, n_nodes, ref_image, interpolation, self.device, chunk_max=chunk)
             slot = FrameSlot(layout, max_iter=10 * self.rounds)
             slot.set_params(tol, alpha_reg)

@@ -122,6 +122,49 @@ def _elements_of(pix) -> np.ndarray:
     return inv.reshape(-1)
 
 
+def _grid_struct(nodes, elements, gc, roi_mask, H: int, W: int, bbox_pad: float, dev):
+    """d2ic_grid_t of a tensor-grid mesh (``gc`` from pixel_assets.grid_cells) and the device
+    tensors it points to (keep them alive while the struct is used)."""
+    from .pixel_assets import _bbox
+    gx, gy, cell, elem_cell = gc
+    T = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt))).to(dev)
+    keep = dict(gx=T(gx, np.float64), gy=T(gy, np.float64), cell=T(cell, np.int32), ec=T(elem_cell, np.int32),
+                el=T(elements, np.int32), nodes=T(nodes, np.float64))
+    if roi_mask is not None:
+        rm = np.asarray(roi_mask, dtype=bool)
+        if rm.shape != (H, W):
+            raise ValueError(f"roi_mask shape {rm.shape} does not match ref_image shape {(H, W)}")
+        keep["roi"] = T(rm, np.uint8)
+    g = _lib.Grid()
+    g.gx, g.gy, g.nx, g.ny = ptr(keep["gx"]), ptr(keep["gy"]), int(gx.size), int(gy.size)
+    g.cell, g.elem_cell, g.elements, g.nodes = ptr(keep["cell"]), ptr(keep["ec"]), ptr(keep["el"]), ptr(keep["nodes"])
+    g.roi = ptr(keep["roi"]) if "roi" in keep else None
+    g.n_elem, g.n_nodes, g.H, g.W = int(elements.shape[0]), int(nodes.shape[0]), int(H), int(W)
+    g.i0, g.i1, g.j0, g.j1 = _bbox(nodes, H, W, bbox_pad)
+    return g, keep
+
+
+def _grid_counts(g, n_elem: int, dev) -> np.ndarray:
+    """ROI pixels owned by each element (d2ic_grid_count)."""
+    counts = torch.zeros(max(n_elem, 1), dtype=torch.int32, device=dev)
+    _lib.call("d2ic_grid_count", ctypes.byref(g), ptr(counts), _lib.stream_handle())
+    return counts[:n_elem].cpu().numpy().astype(np.int64)
+
+
+def grid_element_counts(mesh, roi_mask, image_shape, bbox_pad: float = 2.0, binning: float = 1.0, device=None):
+    """ROI pixels of each element of a tensor-grid mesh, counted on the device."""
+    from .pixel_assets import grid_cells
+    dev = torch.device(device if device is not None else "cuda")
+    nodes = np.asarray(mesh.nodes_xy, dtype=np.float64) / float(binning)
+    elements = np.asarray(mesh.elements, dtype=np.int64)
+    gc = grid_cells(nodes, elements)
+    if gc is None:
+        raise ValueError("grid_element_counts needs a tensor-grid mesh with one element per cell")
+    H, W = (int(v) for v in image_shape)
+    g, keep = _grid_struct(nodes, elements, gc, roi_mask, H, W, bbox_pad, dev)
+    return _grid_counts(g, int(elements.shape[0]), dev)
+
+
 class FrameLayout:
     """Device-resident static data of one (reference image, mesh) pair."""
 
@@ -130,6 +173,12 @@ class FrameLayout:
         if not 1 <= int(chunk_max) <= _lib.CHUNK_MAX:
             raise ValueError(f"chunk_max must be in [1, {_lib.CHUNK_MAX}]")
         chunk_max = int(chunk_max)
+        from .pixel_assets import GridPixelData
+        if isinstance(pix, GridPixelData) and pix.device_ok():
+            built = FrameLayout.from_grid(pix.mesh, pix.roi_mask, ref_image, interpolation, device, chunk_max,
+                                          bbox_pad=pix.bbox_pad, binning=pix.binning)
+            self.__dict__.update(built.__dict__)
+            return
         self.device = torch.device(device if device is not None else "cuda")
         self.kind = interp_kind(interpolation)
         self.n_nodes = int(n_nodes)
@@ -246,19 +295,105 @@ class FrameLayout:
                       self.kind, ptr(self.pix), _lib.stream_handle())
         self.ref_image = ref
         del ref_coeff
-        # shared-memory coefficient tile per chunk (cubic): the chunk's largest pixel box plus the
-        # 4x4 stencil (3), a 2-pixel margin each side (4), one pixel of spread between the
-        # element's nodes (1) and, in x, up to 3 columns lost to the 16-byte TMA alignment
-        self.tile_w = self.tile_h = 0
-        if self.kind == _lib.INTERP_CUBIC and self.n_chunks and self.W + 2 * PAD < 32768 and self.H + 2 * PAD < 32768:
-            b0 = chunk_box[:, 0].astype(np.int64) & 0xFFFFFFFF
-            b1 = chunk_box[:, 1].astype(np.int64) & 0xFFFFFFFF
-            cw = int(((b1 & 0xFFFF) - (b0 & 0xFFFF)).max()) + 1
-            ch = int(((b1 >> 16) - (b0 >> 16)).max()) + 1
-            tw = (cw + 11 + 3) // 4 * 4
-            th = ch + 8
-            if tw * th <= _lib.TILE_MAX_FLOATS:
-                self.tile_w, self.tile_h = tw, th
+        self.tile_w, self.tile_h = self._tile_shape(self.kind, chunk_box, self.W, self.H)
+
+    @staticmethod
+    def _tile_shape(kind: int, chunk_box: np.ndarray, W: int, H: int):
+        """Shared-memory coefficient tile per chunk (cubic): the chunk's largest pixel box plus the
+        4x4 stencil (3), a 2-pixel margin each side (4), one pixel of spread between the element's
+        nodes (1) and, in x, up to 3 columns lost to the 16-byte TMA alignment."""
+        if kind != _lib.INTERP_CUBIC or chunk_box.shape[0] == 0 or W + 2 * PAD >= 32768 or H + 2 * PAD >= 32768:
+            return 0, 0
+        b0 = chunk_box[:, 0].astype(np.int64) & 0xFFFFFFFF
+        b1 = chunk_box[:, 1].astype(np.int64) & 0xFFFFFFFF
+        cw = int(((b1 & 0xFFFF) - (b0 & 0xFFFF)).max()) + 1
+        ch = int(((b1 >> 16) - (b0 >> 16)).max()) + 1
+        tw = (cw + 11 + 3) // 4 * 4
+        th = ch + 8
+        return (tw, th) if tw * th <= _lib.TILE_MAX_FLOATS else (0, 0)
+
+    @classmethod
+    def from_grid(cls, mesh, roi_mask, ref_image, interpolation: str = "cubic", device=None,
+                  chunk_max: int = _lib.CHUNK_MAX, bbox_pad: float = 2.0, binning: float = 1.0,
+                  node_reg_weight=None) -> "FrameLayout":
+        """The layout of a tensor-grid mesh built on the device from the ROI mask (d2ic_grid_count,
+        d2ic_grid_layout, d2ic_grid_springs): the same tensors, bit for bit, as building the host
+        pixel assets (build_pixel_assets) and then the layout from them."""
+        from .pixel_assets import grid_cells
+        dev = torch.device(device if device is not None else "cuda")
+        chunk_max = int(chunk_max)
+        if not 1 <= chunk_max <= _lib.CHUNK_MAX:
+            raise ValueError(f"chunk_max must be in [1, {_lib.CHUNK_MAX}]")
+        nodes = np.asarray(mesh.nodes_xy, dtype=np.float64) / float(binning)
+        elements = np.asarray(mesh.elements, dtype=np.int64)
+        gc = grid_cells(nodes, elements)
+        if gc is None:
+            raise ValueError("from_grid needs a tensor-grid mesh with one element per cell")
+        self = cls.__new__(cls)
+        self.device = dev
+        self.kind = interp_kind(interpolation)
+        self.n_nodes = int(nodes.shape[0])
+        ref = as_device_image(ref_image, dev)
+        self.H, self.W = (int(v) for v in ref.shape)
+        if self.H >= 65536 or self.W >= 65536:
+            raise ValueError("image sides must be < 65536")
+        self.cpitch = _pitch(self.W)
+        T = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dt))).to(dev)
+        g, keep = _grid_struct(nodes, elements, gc, roi_mask, self.H, self.W, bbox_pad, dev)
+        s = _lib.stream_handle()
+        Ne = int(elements.shape[0])
+        cnt = _grid_counts(g, Ne, dev)
+        nch = (cnt + chunk_max - 1) // chunk_max
+        off = np.r_[0, np.cumsum(cnt)]
+        choff = np.r_[0, np.cumsum(nch)]
+        Np, n_chunks = int(off[-1]), int(choff[-1])
+        if Np >= 2 ** 31:
+            raise ValueError("too many ROI pixels for one frame")
+        self.n_pix, self.n_chunks = Np, n_chunks
+        self.element_pixel_counts = cnt
+        t_off, t_choff = T(off, np.int32), T(choff, np.int32)
+        ref_coeff = prepare_coefficients(ref, self.kind)
+        self.pix = torch.empty((max(Np, 1), 4), dtype=torch.int32, device=dev)
+        chunk_begin = torch.zeros(n_chunks + 1, dtype=torch.int32, device=dev)
+        chunk_nodes = torch.empty((max(n_chunks, 1), 4), dtype=torch.int32, device=dev)
+        chunk_box = torch.zeros((max(n_chunks, 1), 2), dtype=torch.int32, device=dev)
+        chunk_slot = torch.zeros(max(n_chunks, 1), dtype=torch.int32, device=dev)
+        ng = (self.n_nodes + _lib.NODE_GROUP - 1) // _lib.NODE_GROUP
+        self.group_need = torch.empty(ng, dtype=torch.int32, device=dev)
+        stats = torch.zeros(4, dtype=torch.int32, device=dev)
+        nb = int(_lib.load().d2ic_grid_scratch_bytes(Np, n_chunks))
+        scratch = torch.empty(nb + 256, dtype=torch.uint8, device=dev)
+        sp = (ptr(scratch) + 255) & ~255
+        _lib.call("d2ic_grid_layout", ctypes.byref(g), ptr(t_off), ptr(t_choff), Np, n_chunks, self.kind,
+                  ptr(ref_coeff), self.cpitch, PAD, sp, nb, ptr(self.pix), ptr(chunk_begin), ptr(chunk_nodes),
+                  ptr(chunk_box), ptr(chunk_slot), ptr(self.group_need), ptr(stats), s)
+        st = stats.cpu().numpy()
+        if st[2]:
+            raise ValueError("from_grid: an element has more than 32 chunks; use a larger chunk size")
+        self.node_chunk_k = max(int(st[0]), 1)
+        if self.node_chunk_k > 255:
+            raise ValueError(f"a node touches {self.node_chunk_k} chunks; at most 255 are supported")
+        md = int(st[1])
+        self.max_deg = md
+        rho = (torch.ones(self.n_nodes, dtype=torch.float32, device=dev) if node_reg_weight is None
+               else T(node_reg_weight, np.float32))
+        if md:
+            self.nbr_index = torch.empty((md, self.n_nodes), dtype=torch.int32, device=dev)
+            self.nbr_weight = torch.empty((md, self.n_nodes), dtype=torch.float32, device=dev)
+            _lib.call("d2ic_grid_springs", ctypes.byref(g), ptr(rho), md, ptr(self.nbr_index), ptr(self.nbr_weight), s)
+        else:
+            self.nbr_index = torch.full((1,), -1, dtype=torch.int32, device=dev)
+            self.nbr_weight = torch.zeros((1,), dtype=torch.float32, device=dev)
+        self.chunk_begin = chunk_begin
+        self.chunk_nodes = chunk_nodes[:n_chunks] if n_chunks else torch.zeros((0, 4), dtype=torch.int32, device=dev)
+        self.chunk_box = chunk_box if n_chunks else torch.zeros((1, 2), dtype=torch.int32, device=dev)
+        self.chunk_slot = chunk_slot if n_chunks else torch.zeros((1,), dtype=torch.int32, device=dev)
+        self.pixel_order = None
+        self.ref_image = ref
+        box = chunk_box[:n_chunks].cpu().numpy() if n_chunks else np.zeros((0, 2), np.int32)
+        self.tile_w, self.tile_h = cls._tile_shape(self.kind, box, self.W, self.H)
+        torch.cuda.current_stream(dev).synchronize()        # the scratch and staging tensors go out of scope
+        return self
 
     # bytes read per pixel per objective evaluation by the P phase (pixel record + ~1 coefficient)
     PIX_BYTES = 16 + 4

@@ -87,6 +87,82 @@ def structured_grid(nodes: np.ndarray, elements: np.ndarray):
     return gx, gy, cell
 
 
+def grid_cells(nodes: np.ndarray, elements: np.ndarray):
+    """``(gx, gy, cell, elem_cell)`` for a tensor grid whose every element is a distinct cell (the
+    meshes mask_to_mesh builds), else None; elem_cell[e] = ix | iy << 16 of element e's cell."""
+    sg = structured_grid(nodes, elements)
+    if sg is None:
+        return None
+    gx, gy, cell = sg
+    if gx.size >= 65536 or gy.size >= 65536:
+        return None
+    el = np.asarray(elements, dtype=np.int64)
+    n0 = el[:, 0]
+    iy, ix = n0 // gx.size, n0 % gx.size
+    if not np.array_equal(cell[iy, ix], np.arange(el.shape[0])):      # two elements on one cell
+        return None
+    return gx, gy, cell, (ix | (iy << 16)).astype(np.int64)
+
+
+class GridPixelData:
+    """Pixel assets of a tensor-grid mesh kept as their recipe -- mesh, ROI mask, image shape --
+    for the device layout builder (FrameLayout.from_grid): no per-pixel host array is formed.
+
+    Attribute access to the host fields of :class:`PixelAssets` (``pixel_coords_ref``,
+    ``pixel_shapeN``, ...) builds them once with :func:`build_pixel_assets` (identical values)."""
+
+    def __init__(self, mesh: Mesh, image_shape, roi_mask=None, binning: float = 1.0, bbox_pad: float = 2.0):
+        self.mesh = mesh
+        self.image_shape = tuple(int(v) for v in image_shape)
+        self.roi_mask = None if roi_mask is None else np.asarray(roi_mask, dtype=bool)
+        self.binning = float(binning)
+        self.bbox_pad = float(bbox_pad)
+        self._host = None
+        self._counts = None
+
+    def device_ok(self) -> bool:
+        return _gpu_available() and grid_cells(np.asarray(self.mesh.nodes_xy, np.float64) / self.binning,
+                                              np.asarray(self.mesh.elements, np.int64)) is not None
+
+    def element_pixel_counts(self) -> np.ndarray:
+        """ROI pixels of each element (the device count pass, or the host assets without a GPU)."""
+        if self._counts is None:
+            if self._host is None and self.device_ok():
+                from .engine import grid_element_counts
+                self._counts = grid_element_counts(self.mesh, self.roi_mask, self.image_shape, self.bbox_pad,
+                                                   self.binning)
+            else:
+                e = np.asarray(self.to_host().pixel_elts, np.int64)
+                self._counts = np.bincount(e, minlength=np.asarray(self.mesh.elements).shape[0])
+        return self._counts
+
+    @property
+    def n_pixels(self) -> int:
+        return int(self.element_pixel_counts().sum())
+
+    def to_host(self) -> "PixelAssets":
+        if self._host is None:
+            self._host = build_pixel_assets(self.mesh, np.zeros(self.image_shape, np.float32), self.binning,
+                                            self.roi_mask, self.bbox_pad)
+        return self._host
+
+    def __getattr__(self, name):
+        if name.startswith("_") or name in ("mesh", "image_shape", "roi_mask", "binning", "bbox_pad"):
+            raise AttributeError(name)
+        return getattr(self.to_host(), name)
+
+
+def build_pixel_assets_device(mesh: Mesh, ref_image, binning: float, roi_mask=None, bbox_pad: float = 2.0):
+    """Pixel assets for the device path: a :class:`GridPixelData` recipe when the mesh is a tensor
+    grid and a GPU is present (the solvers then build their layout on the device), else the host
+    :func:`build_pixel_assets`."""
+    H, W = (int(s) for s in np.shape(ref_image)[:2])
+    gp = GridPixelData(mesh, (H, W), roi_mask, binning, bbox_pad)
+    if gp.device_ok():
+        return gp
+    return build_pixel_assets(mesh, ref_image, binning, roi_mask, bbox_pad)
+
+
 def _structured_assign(pc: np.ndarray, gx, gy, cell):
     """Lowest element index whose closed cell rectangle contains each pixel, -1 if none."""
     nx, ny = gx.size, gy.size

@@ -197,6 +197,41 @@ D2IC_API int d2ic_local_coordinates(const double *pixel_coords, const int *pixel
 D2IC_API int d2ic_structured_assign(const double *pixel_coords, long long n_pix, const double *gx, int nx,
                                     const double *gy, int ny, const long long *cell, long long *elts, void *stream);
 
+/* ---- frame layout built on the device from the ROI mask, for the tensor-grid meshes of
+ *      mask_to_mesh (replaces build_pixel_assets, d2ic/pixel_assets.py:21-131,135-294,330-409, and the
+ *      host layout of the engine: the same pixels, element map, Newton coordinates, chunks, node slots
+ *      and spring tables, bit for bit) ---- */
+typedef struct d2ic_grid {
+    const double *gx, *gy;          /* nx, ny grid lines, ascending (device)                       */
+    int nx, ny;
+    const int *cell;                /* (ny - 1) x (nx - 1): element of the cell, -1 for none (device) */
+    const int *elem_cell;           /* n_elem: ix | iy << 16, the element's cell (device)            */
+    const int *elements;            /* n_elem x 4 nodes, Q4 order (device)                           */
+    const double *nodes;            /* n_nodes x 2 coordinates, node iy * nx + ix (device)           */
+    const unsigned char *roi;       /* H x W ROI mask (device), NULL for every pixel                 */
+    int n_elem, n_nodes, H, W;
+    int i0, i1, j0, j1;             /* the padded node bbox [i0, i1) x [j0, j1) of the host sampler  */
+} d2ic_grid_t;
+
+/* Pass 1: the ROI pixels each element owns (lowest element index whose closed cell holds the pixel
+ * centre).  grid: HOST pointer to the descriptor; elem_count: n_elem ints (device). */
+D2IC_API int d2ic_grid_count(const d2ic_grid_t *grid, int *elem_count, void *stream);
+/* Bytes of scratch d2ic_grid_layout needs. */
+D2IC_API size_t d2ic_grid_scratch_bytes(long long n_pix, int n_chunks);
+/* Pass 2: the layout.  elem_off (n_elem + 1) pixel offsets and elem_choff (n_elem + 1) chunk offsets
+ * are the exclusive prefix sums of the counts and of ceil(count / chunk_max) (device).  Writes the
+ * pixel records, chunk_begin (n_chunks + 1), chunk_nodes, chunk_box, chunk_slot, group_need
+ * (ceil(n_nodes / 32)) and stats[4] = {most chunks at one node, largest spring degree, error, 0};
+ * error != 0 when an element has more than 32 chunks. */
+D2IC_API int d2ic_grid_layout(const d2ic_grid_t *grid, const int *elem_off, const int *elem_choff, long long n_pix,
+                              int n_chunks, int kind, const float *ref_coeff, int cpitch, int pad, void *scratch,
+                              size_t scratch_bytes, d2ic_pixrec_t *pix, int *chunk_begin, int *chunk_nodes,
+                              int *chunk_box, int *chunk_slot, int *group_need, int *stats, void *stream);
+/* Pass 3: spring tables (max_deg x n_nodes, column-major, -1 / 0 padded) with rho: n_nodes node
+ * regularisation weights (device). */
+D2IC_API int d2ic_grid_springs(const d2ic_grid_t *grid, const float *rho, int max_deg, int *nbr_index,
+                               float *nbr_weight, void *stream);
+
 /* ---- local Gauss-Newton refinement (replaces LocalGaussNewtonSolver,
  *      d2ic/solver_local_gn.py:34-414) ---- */
 

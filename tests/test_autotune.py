@@ -35,6 +35,16 @@ def test_signature_and_cache_roundtrip(tmp_path):
         Autotuner(device="cpu", chunk_candidates=(0, 300))
 
 
+def test_only_distinct_chunk_sizes_are_timed():
+    """Chunks hold pixels of one element: sizes at or above the largest element give one layout."""
+    from d2ic_gb300.autotune import distinct_chunk_sizes
+    assert distinct_chunk_sizes((64, 128, 256), 64) == (64,)          # 8-px elements
+    assert distinct_chunk_sizes((64, 128, 256), 144) == (64, 128, 256)   # 12-px elements
+    assert distinct_chunk_sizes((64, 128, 256), 256) == (64, 128, 256)
+    assert distinct_chunk_sizes((64, 128, 256), 1024) == (64, 128, 256)
+    assert distinct_chunk_sizes((256,), 16) == (256,)
+
+
 @pytest.mark.gpu
 def test_tuned_solve_matches_oracle(cuda):
     import d2ic_gb300 as d2

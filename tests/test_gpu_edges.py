@@ -63,10 +63,9 @@ def test_start_at_the_solution_stops_on_the_first_evaluation(cuda):
 @pytest.mark.parametrize("interpolation", ["linear", "cubic"])
 def test_ragged_image_matches_oracle(cuda, interpolation):
     """257 x 389 image, 12-px elements over a centred 240 x 372 ROI: no element size divides the
-    image, rows and pitch are odd.  The ROI is element-aligned (the nodes of a partly covered
-    corner element are held too weakly for an FP32 solve to reach the FP64 minimum within
-    1e-3 px), and the tolerance is the headline one (1e-3): below ~1e-4 the FP32 pixel sums of the
-    objective cannot resolve the Armijo decrease, as in the reference's FP32 solve."""
+    image, rows and pitch are odd.  The tolerance is the headline one (1e-3): below ~1e-4 the FP32
+    pixel sums of the objective cannot resolve the Armijo decrease, as in the reference's FP32
+    solve.  (Partly covered elements are covered by tests/test_gpu_parity_masks.py.)"""
     import d2ic_gb300 as d2
     from d2ic_gb300.synthetic import Translation
     from oracle import fast
