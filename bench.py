@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--serve-frames", type=int, default=4)
     p.add_argument("--serve-slots", type=int, default=32)
     p.add_argument("--serve-slice", type=int, default=16)
+    p.add_argument("--no-4096", action="store_true", help="skip the 4096^2 engine measurement")
+    p.add_argument("--frames-4096", type=int, default=3)
     p.add_argument("--no-stream", action="store_true", help="skip the serving stream")
     p.add_argument("--stream-frames", type=int, default=4096)
     p.add_argument("--stream-seqs", type=int, default=128)
@@ -813,6 +815,43 @@ def run_adjoint(args, dev):
 
 
 # ---------------------------------------------------------------------------
+# the engine at 4096^2 (frame data larger than L2: the HBM-bound case)
+# ---------------------------------------------------------------------------
+
+def run_engine_4096(args, dev):
+    """The plate-hole sequence scaled to 4096^2 (11.8 M ROI pixels, 66,049 nodes): frames 1..n
+    warm-started, engine launches timed with CUDA events on their stream, L2 flushed between
+    steps; the same algorithmic bytes as the headline roofline."""
+    import torch
+
+    import d2ic_gb300 as d2
+    from d2ic_gb300.sequence import SequenceRunner
+    wl = make_workload("plate_hole_4096", 1 + args.frames_4096, 1, dev)
+    solver = d2.GlobalCGSolver(device=dev)
+    dic = d2.DICMeshBased(wl.mesh, solver, wl.config)
+    dic.prepare(wl.ref, wl.assets)
+    runner = SequenceRunner(solver, dic.state)
+    frames_dev = [torch.from_numpy(f).to(dev) for f in wl.frames]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    runner.run(frames_dev, init_cfg=wl.init, propagation="previous")              # warm-up
+    ms, evals = [], []
+    for _ in range(max(1, min(args.steps, 3))):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        res = runner.run(frames_dev, init_cfg=wl.init, propagation="previous", time_engine=True)
+        torch.cuda.synchronize()
+        ms.extend(a.elapsed_time(b) for a, b in res.engine_events)
+        evals.extend(res.info[:, 2].cpu().tolist())
+    peak, peak_src = peaks()
+    bpe = B_PIX * wl.n_pix + B_NODE * wl.n_nodes
+    achieved = (sum(evals) * bpe / 1e9) / (sum(ms) / 1000.0)
+    return {"workload": wl.name, "frames": len(frames_dev), "roi_pixels": wl.n_pix, "nodes": wl.n_nodes,
+            "launch_ms_mean": statistics.mean(ms), "evals_per_launch": statistics.mean(evals),
+            "us_per_eval": 1000.0 * sum(ms) / sum(evals), "bytes_per_eval": bpe, "achieved_GBps": achieved,
+            "peak_GBps": peak, "peak_source": peak_src, "frac": achieved / peak}
+
+
+# ---------------------------------------------------------------------------
 # GPU leg
 # ---------------------------------------------------------------------------
 
@@ -923,6 +962,8 @@ def run_ours(args, ws, rank, local):
         u_api = np.stack([np.asarray(r.u_nodal) for r in res_b.results])
         out["e2e"]["max_abs_diff_vs_value_path_px"] = float(np.abs(u_dev - u_api).max())
 
+    if not args.no_4096:
+        out["engine_4096"] = run_engine_4096(args, dev)
     if not args.no_stream:
         out["serving_stream"] = run_serving_stream(args, dev)
     if not args.no_serve:
