@@ -66,6 +66,9 @@ def parse():
     p.add_argument("--stream-frames", type=int, default=4096)
     p.add_argument("--stream-seqs", type=int, default=128)
     p.add_argument("--stream-plain-frames", type=int, default=4096)
+    p.add_argument("--stream-slots", type=int, default=64,
+                   help="frames in flight in the server (the engine keeps up to 64 active frames' lookup "
+                        "tables in shared memory)")
     p.add_argument("--stream-rates", type=lambda v: [float(x) for x in v.split(",")],
                    default=[50.0, 100.0, 200.0, 500.0, 1000.0, 2000.0])
     p.add_argument("--stream-window", type=float, default=20.0,
@@ -515,7 +518,7 @@ def run_serving_stream(args, dev):
     plain_fps = n_plain / t_plain
 
     t0 = time.perf_counter()
-    srv = DICServer(dev, ServeConfig(max_slots=min(len(seqs), 128), slice_rounds=args.serve_slice))
+    srv = DICServer(dev, ServeConfig(max_slots=min(len(seqs), args.stream_slots), slice_rounds=args.serve_slice))
     for q in seqs:
         srv.add_sequence(q.seq_id, q.ref, q.mesh, q.assets, q.config, init=q.init)
     t_srv_setup = time.perf_counter() - t0
@@ -538,7 +541,12 @@ def run_serving_stream(args, dev):
     reqs, t_sat = served(N)
     served_fps = N / t_sat
     done = {(r.seq_id, r.frame_index): r for r in reqs}
-    diff = max(float(np.abs(done[key].u - u).max()) for key, u in plain_u.items())
+    diffs = {key: float(np.abs(done[key].u - u).max()) for key, u in plain_u.items()}
+    diff = max(diffs.values())
+    side_of = {q.seq_id: q.side for q in seqs}
+    svc_by_side = {}
+    for (s_id, _k), t in zip(st.order[:n_plain], svc):
+        svc_by_side.setdefault(side_of[s_id], []).append(t)
     it_capped = sum(1 for r in reqs if r.n_iters is not None and r.n_iters >= seqs[r.seq_id].config.max_iters)
     sweep = []
     for rate in args.stream_rates:
@@ -565,8 +573,14 @@ def run_serving_stream(args, dev):
             "plain_frames_per_s": plain_fps, "plain_frames_timed": n_plain,
             "plain_service_ms_p50": 1000 * float(np.percentile(svc, 50)),
             "served_frames_per_s": served_fps, "speedup": served_fps / plain_fps,
-            "max_abs_diff_vs_plain_px": diff, "frames_at_max_iters": it_capped,
-            "rate_sweep": sweep, "parity_sampled": parity, "slots": min(len(seqs), 128),
+            "max_abs_diff_vs_plain_px": diff,
+            "frames_differing_from_plain": int(sum(v > 0 for v in diffs.values())),
+            "max_abs_diff_vs_plain_first_frames_px": max([v for (s_id, k), v in diffs.items() if k == 0], default=0.0),
+            "plain_service_ms_p50_by_side": {str(k): 1000 * float(np.percentile(v, 50))
+                                             for k, v in sorted(svc_by_side.items())},
+            "plain_seconds_by_side": {str(k): float(np.sum(v)) for k, v in sorted(svc_by_side.items())},
+            "frames_at_max_iters": it_capped,
+            "rate_sweep": sweep, "parity_sampled": parity, "slots": min(len(seqs), args.stream_slots),
             "slice_rounds": args.serve_slice, "graphs": sorted(srv.graphs), "long_slices": srv.long_slices,
             "setup_s": {"stream": round(t_build, 1), "plain": round(t_plain_setup, 1),
                         "server": round(t_srv_setup, 1)},
