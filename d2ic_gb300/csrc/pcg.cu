@@ -14,10 +14,10 @@
 // columns.  This replaces the chunk -> node-slot -> node pass per product (one
 // write and one read of node_chunk_k * Nn * 2 * K floats per product).
 //
-// PCG: per iteration three kernels -- AP = H P with the column sums P.AP fused,
-// the update of X, R, Z with the sums R.R and R.Z fused, the new direction --
-// each column sum a per-block partial reduced by the last block to finish, in
-// block order (deterministic).  The step kernel also decides convergence
+// PCG: per iteration AP = H P with the block partials of P.AP, their column sums,
+// the update of X, R, Z with the partials of R.R and R.Z, their column sums (one
+// warp per column, blocks summed in a fixed order: deterministic) and the new
+// direction.  The last block of the second column sum decides convergence
 // (||R|| <= rtol ||B|| for every column) into a device flag that makes the later
 // kernels return at once, so the host launches iterations in batches and reads
 // the flag once per batch instead of synchronising every iteration.
@@ -187,42 +187,87 @@ __global__ void __launch_bounds__(256) hop_apply(const int *__restrict__ idx, co
     }
 }
 
+// The entries of a block's 8 nodes, staged in shared memory and read as broadcasts.
+struct HopTile {
+    int idx[8][HOP];
+    float4 blk[8][HOP];
+    int cnt[8];
+};
+
+__device__ __forceinline__ void hop_stage(const int *__restrict__ idx, const float4 *__restrict__ blk, int n_nodes,
+                                          HopTile &T) {
+    static_assert(8 * HOP <= 256, "one thread per staged entry");
+    const int t = threadIdx.x;
+    if (t < 8 * HOP) {
+        const int w = t / HOP, q = t % HOP, n = blockIdx.x * 8 + w;
+        int j = -1;
+        float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (n < n_nodes) {
+            j = __ldg(idx + (size_t)n * HOP + q);
+            b = __ldg(blk + (size_t)n * HOP + q);
+        }
+        T.idx[w][q] = j;
+        T.blk[w][q] = b;
+    }
+    __syncthreads();
+    if (t < 8) {
+        int c = 0;
+        while (c < HOP && T.idx[t][c] >= 0) ++c;   // entries are packed from the first
+        T.cnt[t] = c;
+    }
+    __syncthreads();
+}
+
+// node w of the tile x 4 consecutive columns k0 .. k0 + 3 (K a multiple of 4): the same operations per
+// column, in the same order, as hop_row
+__device__ __forceinline__ void hop_row4(const HopTile &T, int w, int K, int k0, const float *__restrict__ V,
+                                         float4 &yx, float4 &yy) {
+    yx = make_float4(0.f, 0.f, 0.f, 0.f);
+    yy = yx;
+    const int cnt = T.cnt[w];
+#pragma unroll 3
+    for (int q = 0; q < cnt; ++q) {
+        const int j = T.idx[w][q];
+        const float4 b = T.blk[w][q];
+        const float4 vx = __ldg(reinterpret_cast<const float4 *>(V + ((size_t)j * 2) * K + k0));
+        const float4 vy = __ldg(reinterpret_cast<const float4 *>(V + ((size_t)j * 2 + 1) * K + k0));
+        yx.x = __fmaf_rn(b.x, vx.x, __fmaf_rn(b.y, vy.x, yx.x));
+        yx.y = __fmaf_rn(b.x, vx.y, __fmaf_rn(b.y, vy.y, yx.y));
+        yx.z = __fmaf_rn(b.x, vx.z, __fmaf_rn(b.y, vy.z, yx.z));
+        yx.w = __fmaf_rn(b.x, vx.w, __fmaf_rn(b.y, vy.w, yx.w));
+        yy.x = __fmaf_rn(b.y, vx.x, __fmaf_rn(b.z, vy.x, yy.x));
+        yy.y = __fmaf_rn(b.y, vx.y, __fmaf_rn(b.z, vy.y, yy.y));
+        yy.z = __fmaf_rn(b.y, vx.z, __fmaf_rn(b.z, vy.z, yy.z));
+        yy.w = __fmaf_rn(b.y, vx.w, __fmaf_rn(b.z, vy.w, yy.w));
+    }
+}
+
+// Y = H V for K a multiple of 4: block = 8 nodes (warps) x 128 columns (4 per lane)
+__global__ void __launch_bounds__(256) hop_apply4(const int *__restrict__ idx, const float4 *__restrict__ blk,
+                                                  int n_nodes, const float *__restrict__ V, int K,
+                                                  float *__restrict__ Y) {
+    __shared__ HopTile T;
+    hop_stage(idx, blk, n_nodes, T);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n = blockIdx.x * 8 + w, k0 = blockIdx.y * 128 + 4 * lane;
+    if (n >= n_nodes || k0 >= K) return;
+    float4 yx, yy;
+    hop_row4(T, w, K, k0, V, yx, yy);
+    *reinterpret_cast<float4 *>(Y + ((size_t)n * 2) * K + k0) = yx;
+    *reinterpret_cast<float4 *>(Y + ((size_t)n * 2 + 1) * K + k0) = yy;
+}
+
 // ---------------------------------------------------------------------------
 // PCG
 // ---------------------------------------------------------------------------
 struct PcgCtl {
     int done;        // all columns converged: later kernels return at once
     int iters;       // iterations whose update ran
-    int cnt_step;    // last-block counters (reset by the last block)
-    int cnt_init;
-    int cnt_pap[1];  // one per 32-column tile (variable length, at the end)
+    int cnt_check;   // last-block counter of the convergence check (reset by the last block)
+    int pad_;
 };
 
 __device__ __forceinline__ int ld_flag(const int *p) { return *(volatile const int *)p; }
-
-// the last block to arrive (after writing its partials) returns true; the counter is reset
-__device__ __forceinline__ bool last_block(int *cnt, int nblocks) {
-    __shared__ int s_last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const int t = atomicAdd(cnt, 1);
-        s_last = t == nblocks - 1;
-        if (s_last) *cnt = 0;
-    }
-    __syncthreads();
-    if (s_last) __threadfence();
-    return s_last;
-}
-
-// out[k] = sum over blocks b (in order) of part[b * K + k], whole block, columns k0 .. k1-1
-__device__ void reduce_cols(const double *part, int nb, int K, int k0, int k1, double *out) {
-    for (int k = k0 + (int)threadIdx.x; k < k1; k += blockDim.x) {
-        double s = 0.0;
-        for (int b = 0; b < nb; ++b) s += __ldcg(part + (size_t)b * K + k);
-        out[k] = s;
-    }
-}
 
 // nodes [n0, n1) of block b
 __device__ __forceinline__ void node_range(int n_nodes, int &n0, int &n1) {
@@ -235,8 +280,7 @@ __global__ void __launch_bounds__(PT) pcg_init(int n_nodes, int K, const double 
                                                const unsigned char *__restrict__ act, const double *__restrict__ Minv,
                                                double *__restrict__ X, double *__restrict__ R, double *__restrict__ Z,
                                                double *__restrict__ P, float *__restrict__ Pf,
-                                               double *__restrict__ part_rz, double *__restrict__ part_bb,
-                                               double *__restrict__ rz, double *__restrict__ bb, PcgCtl *ctl) {
+                                               double *__restrict__ part_rz, double *__restrict__ part_bb) {
     int n0, n1;
     node_range(n_nodes, n0, n1);
     for (int k = threadIdx.x; k < K; k += PT) {
@@ -263,44 +307,71 @@ __global__ void __launch_bounds__(PT) pcg_init(int n_nodes, int K, const double 
         part_rz[(size_t)blockIdx.x * K + k] = srz;
         part_bb[(size_t)blockIdx.x * K + k] = sbb;
     }
-    if (last_block(&ctl->cnt_init, gridDim.x)) {
-        reduce_cols(part_rz, gridDim.x, K, 0, K, rz);
-        reduce_cols(part_bb, gridDim.x, K, 0, K, bb);
-    }
 }
 
-// AP = H P (masked to active dofs) and pap[k] = P.AP: block = 8 nodes x 32 columns
+// AP = H P (masked to active dofs) and the block partials of pap[k] = P.AP: block = 8 nodes x
+// 32 columns (one per lane) or, with VEC (K a multiple of 4), 128 columns (four per lane)
+template <bool VEC>
 __global__ void __launch_bounds__(256) pcg_apply(const int *__restrict__ idx, const float4 *__restrict__ blk,
                                                  int n_nodes, int K, const float *__restrict__ Pf,
                                                  const double *__restrict__ P, const unsigned char *__restrict__ act,
                                                  float *__restrict__ AP, double *__restrict__ part,
-                                                 double *__restrict__ pap, PcgCtl *ctl) {
+                                                 const PcgCtl *ctl) {
     if (ld_flag(&ctl->done)) return;
-    __shared__ double s_p[8][32];
+    constexpr int CW = VEC ? 4 : 1;                 // columns per lane
+    __shared__ HopTile T;
+    __shared__ double s_p[8][32 * CW];
+    hop_stage(idx, blk, n_nodes, T);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int n = blockIdx.x * 8 + w, k = blockIdx.y * 32 + lane;
-    double pp = 0.0;
-    if (n < n_nodes) {
-        float yx, yy;
-        hop_row(idx, blk, n, K, k, Pf, lane, yx, yy);
-        if (k < K) {
-            const size_t i0 = ((size_t)n * 2) * K + k, i1 = i0 + K;
-            AP[i0] = yx;
-            AP[i1] = yy;
-            if (act[n]) pp = P[i0] * (double)yx + P[i1] * (double)yy;
+    const int n = blockIdx.x * 8 + w, k0 = blockIdx.y * 32 * CW + CW * lane;
+    double pp[CW];
+#pragma unroll
+    for (int c = 0; c < CW; ++c) pp[c] = 0.0;
+    if (n < n_nodes && k0 < K) {
+        float y0[CW], y1[CW];
+        if (VEC) {
+            float4 yx, yy;
+            hop_row4(T, w, K, k0, Pf, yx, yy);
+            *reinterpret_cast<float4 *>(AP + ((size_t)n * 2) * K + k0) = yx;
+            *reinterpret_cast<float4 *>(AP + ((size_t)n * 2 + 1) * K + k0) = yy;
+            const float a0[4] = {yx.x, yx.y, yx.z, yx.w}, a1[4] = {yy.x, yy.y, yy.z, yy.w};
+#pragma unroll
+            for (int c = 0; c < CW; ++c) {
+                y0[c] = a0[c];
+                y1[c] = a1[c];
+            }
+        } else {
+            float yx = 0.f, yy = 0.f;
+            for (int q = 0; q < T.cnt[w]; ++q) {
+                const int j = T.idx[w][q];
+                const float4 b = T.blk[w][q];
+                const float vx = __ldg(Pf + ((size_t)j * 2) * K + k0), vy = __ldg(Pf + ((size_t)j * 2 + 1) * K + k0);
+                yx = __fmaf_rn(b.x, vx, __fmaf_rn(b.y, vy, yx));
+                yy = __fmaf_rn(b.y, vx, __fmaf_rn(b.z, vy, yy));
+            }
+            AP[((size_t)n * 2) * K + k0] = yx;
+            AP[((size_t)n * 2 + 1) * K + k0] = yy;
+            y0[0] = yx;
+            y1[0] = yy;
+        }
+        if (act[n]) {
+#pragma unroll
+            for (int c = 0; c < CW; ++c) {
+                const size_t i0 = ((size_t)n * 2) * K + k0 + c;
+                pp[c] = P[i0] * (double)y0[c] + P[i0 + K] * (double)y1[c];
+            }
         }
     }
-    s_p[w][lane] = pp;
-    __syncthreads();
-    if (w == 0) {
-        double s = 0.0;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) s += s_p[i][lane];
-        if (k < K) part[(size_t)blockIdx.x * K + k] = s;
-    }
-    if (last_block(&ctl->cnt_pap[blockIdx.y], gridDim.x)) {
-        const int k0 = blockIdx.y * 32, k1 = min(k0 + 32, K);
-        reduce_cols(part, gridDim.x, K, k0, k1, pap);
+    for (int c = 0; c < CW; ++c) s_p[w][CW * lane + c] = pp[c];
+    __syncthreads();
+    for (int t = threadIdx.x; t < 32 * CW; t += blockDim.x) {
+        const int k = blockIdx.y * 32 * CW + t;
+        if (k >= K) continue;
+        double sum = 0.0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) sum += s_p[i][t];
+        part[(size_t)blockIdx.x * K + k] = sum;
     }
 }
 
@@ -310,8 +381,7 @@ __global__ void __launch_bounds__(PT) pcg_step(int n_nodes, int K, const double 
                                                double *__restrict__ R, double *__restrict__ Z,
                                                const double *__restrict__ P, const float *__restrict__ AP,
                                                double *__restrict__ part_rr, double *__restrict__ part_rz,
-                                               double *__restrict__ rr, double *__restrict__ rz_new,
-                                               const double *__restrict__ bb, double rtol, PcgCtl *ctl) {
+                                               const PcgCtl *ctl) {
     if (ld_flag(&ctl->done)) return;
     int n0, n1;
     node_range(n_nodes, n0, n1);
@@ -336,20 +406,50 @@ __global__ void __launch_bounds__(PT) pcg_step(int n_nodes, int K, const double 
         part_rr[(size_t)blockIdx.x * K + k] = srr;
         part_rz[(size_t)blockIdx.x * K + k] = srz;
     }
-    if (last_block(&ctl->cnt_step, gridDim.x)) {
-        reduce_cols(part_rr, gridDim.x, K, 0, K, rr);
-        reduce_cols(part_rz, gridDim.x, K, 0, K, rz_new);
-        __syncthreads();
-        int ok = 1;
-        for (int k = threadIdx.x; k < K; k += PT) {
-            const double bn = fmax(sqrt(__ldcg(bb + k)), 1e-300);
-            ok &= sqrt(__ldcg(rr + k)) <= rtol * bn;
+}
+
+// out_a[k] (and out_b[k]) = sum over blocks b of part_a[b][k] (part_b): one warp per column, lane l
+// sums blocks l, l + 32, ... in order, then a fixed shuffle tree (deterministic).  With `check`,
+// the last block to finish decides convergence (every column: sqrt(out_a) <= rtol sqrt(bb)) and
+// counts the iteration.
+__global__ void pcg_colsum(int nb, int K, const double *__restrict__ part_a, const double *__restrict__ part_b,
+                           double *__restrict__ out_a, double *__restrict__ out_b, const double *__restrict__ bb,
+                           double rtol, int check, PcgCtl *ctl) {
+    if (ld_flag(&ctl->done)) return;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (k < K) {
+        double sa = 0.0, sb = 0.0;
+        for (int b = lane; b < nb; b += 32) {
+            sa += part_a[(size_t)b * K + k];
+            if (part_b) sb += part_b[(size_t)b * K + k];
         }
-        ok = __syncthreads_and(ok);
-        if (threadIdx.x == 0) {
-            ctl->iters += 1;
-            if (ok) ctl->done = 1;
+        sa = warp_sum_d(sa);
+        sb = warp_sum_d(sb);
+        if (lane == 0) {
+            out_a[k] = sa;
+            if (out_b) out_b[k] = sb;
         }
+    }
+    if (!check) return;
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_last = atomicAdd(&ctl->cnt_check, 1) == (int)gridDim.x - 1;
+        if (s_last) ctl->cnt_check = 0;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    int ok = 1;
+    for (int c = threadIdx.x; c < K; c += blockDim.x) {
+        const double bn = fmax(sqrt(__ldcg(bb + c)), 1e-300);
+        ok &= sqrt(__ldcg(out_a + c)) <= rtol * bn;
+    }
+    ok = __syncthreads_and(ok);
+    if (threadIdx.x == 0) {
+        ctl->iters += 1;
+        if (ok) ctl->done = 1;
     }
 }
 
@@ -406,7 +506,7 @@ static size_t carve(int n_nodes, int K, int node_chunk_k, char *base, PcgWork *w
     w->pap = (double *)take(sizeof(double) * K);
     w->rr = (double *)take(sizeof(double) * K);
     w->bb = (double *)take(sizeof(double) * K);
-    w->ctl = (PcgCtl *)take(sizeof(PcgCtl) + sizeof(int) * (size_t)((K + 31) / 32));
+    w->ctl = (PcgCtl *)take(sizeof(PcgCtl));
     HopView hv;
     w->op = take(hop_layout(n_nodes, node_chunk_k, nullptr, &hv));
     return off;
@@ -468,9 +568,15 @@ extern "C" int d2ic_hessian_apply(const void *op, int n_nodes, int node_chunk_k,
     D2IC_REQUIRE(op && V && Y && n_nodes >= 1 && K >= 1 && node_chunk_k >= 1, "d2ic_hessian_apply: bad arguments");
     HopView hv;
     hop_layout(n_nodes, node_chunk_k, (char *)op, &hv);
-    hop_apply<<<dim3((unsigned)((n_nodes + 7) / 8), (unsigned)((K + 31) / 32)), 256, 0, (cudaStream_t)stream>>>(
-        hv.idx, hv.blk, n_nodes, V, K, Y);
-    D2IC_CHECK_LAUNCH("hop_apply");
+    if (K % 4 == 0 && ((uintptr_t)V & 15) == 0 && ((uintptr_t)Y & 15) == 0) {
+        hop_apply4<<<dim3((unsigned)((n_nodes + 7) / 8), (unsigned)((K + 127) / 128)), 256, 0,
+                     (cudaStream_t)stream>>>(hv.idx, hv.blk, n_nodes, V, K, Y);
+        D2IC_CHECK_LAUNCH("hop_apply4");
+    } else {
+        hop_apply<<<dim3((unsigned)((n_nodes + 7) / 8), (unsigned)((K + 31) / 32)), 256, 0, (cudaStream_t)stream>>>(
+            hv.idx, hv.blk, n_nodes, V, K, Y);
+        D2IC_CHECK_LAUNCH("hop_apply");
+    }
     return D2IC_OK;
 }
 
@@ -497,16 +603,18 @@ extern "C" int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n
     HopView hv;
     int st = assemble(frame_dev, n_chunks, n_nodes, node_chunk_k, chunk_hess, inv_np, alpha_reg, w.op, s, &hv);
     if (st) return st;
-    const size_t ctl_bytes = sizeof(PcgCtl) + sizeof(int) * (size_t)((K + 31) / 32);
-    cudaError_t e = cudaMemsetAsync(w.ctl, 0, ctl_bytes, s);
+    cudaError_t e = cudaMemsetAsync(w.ctl, 0, sizeof(PcgCtl), s);
     if (e != cudaSuccess) return cuda_status(e, "pcg control");
     const int nb = pcg_blocks(n_nodes);
-    pcg_init<<<nb, PT, 0, s>>>(n_nodes, K, B, active, Minv, X, w.R, w.Z, w.P, w.Pf, w.part_a, w.part_b, w.rz, w.bb,
-                               w.ctl);
+    const int rb = (K + 7) / 8;                      // column sums: 8 warps (columns) per block
+    pcg_init<<<nb, PT, 0, s>>>(n_nodes, K, B, active, Minv, X, w.R, w.Z, w.P, w.Pf, w.part_a, w.part_b);
+    pcg_colsum<<<rb, 256, 0, s>>>(nb, K, w.part_a, w.part_b, w.rz, w.bb, nullptr, 0.0, 0, w.ctl);
     D2IC_CHECK_LAUNCH("pcg init");
     st = check_overflow(hv, s);                      // also waits for the assembly
     if (st) return st;
-    const dim3 ag((unsigned)((n_nodes + 7) / 8), (unsigned)((K + 31) / 32));
+    const bool vec = K % 4 == 0;                     // Pf and AP are 256-byte aligned
+    const int na = (n_nodes + 7) / 8;
+    const dim3 ag((unsigned)na, (unsigned)(vec ? (K + 127) / 128 : (K + 31) / 32));
     constexpr int BATCH = 8;                         // iterations launched per host check of the flag
     int it = 0;
     PcgCtl host_ctl = {};
@@ -514,9 +622,15 @@ extern "C" int d2ic_pcg_solve(const d2ic_frame_t *frame_dev, int n_chunks, int n
     while (it < max_iter) {
         const int nb_it = max_iter - it < BATCH ? max_iter - it : BATCH;
         for (int i = 0; i < nb_it; ++i) {
-            pcg_apply<<<ag, 256, 0, s>>>(hv.idx, hv.blk, n_nodes, K, w.Pf, w.P, active, w.AP, w.part_a, w.pap, w.ctl);
+            if (vec)
+                pcg_apply<true><<<ag, 256, 0, s>>>(hv.idx, hv.blk, n_nodes, K, w.Pf, w.P, active, w.AP, w.part_a, w.ctl);
+            else
+                pcg_apply<false><<<ag, 256, 0, s>>>(hv.idx, hv.blk, n_nodes, K, w.Pf, w.P, active, w.AP, w.part_a,
+                                                    w.ctl);
+            pcg_colsum<<<rb, 256, 0, s>>>(na, K, w.part_a, nullptr, w.pap, nullptr, nullptr, 0.0, 0, w.ctl);
             pcg_step<<<nb, PT, 0, s>>>(n_nodes, K, rz, w.pap, active, Minv, X, w.R, w.Z, w.P, w.AP, w.part_a,
-                                       w.part_b, w.rr, rz_new, w.bb, rtol, w.ctl);
+                                       w.part_b, w.ctl);
+            pcg_colsum<<<rb, 256, 0, s>>>(nb, K, w.part_a, w.part_b, w.rr, rz_new, w.bb, rtol, 1, w.ctl);
             pcg_dir<<<nb, PT, 0, s>>>(n_nodes, K, rz, rz_new, w.Z, w.P, w.Pf, w.ctl);
             double *t = rz;
             rz = rz_new;

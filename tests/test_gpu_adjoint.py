@@ -125,3 +125,19 @@ def test_assembled_operator_equals_chunk_matvec(problem, K):
     b = adj.matvec_chunks(V)
     scale = float(b.abs().max())
     assert float((a - b).abs().max()) <= 1e-5 * scale
+
+
+def test_pcg_solves_with_four_column_tiles(problem):
+    """K a multiple of 4 takes the vectorised product inside the PCG; each column's solution must
+    equal the one-column solve (the same operations per column), and H X = B must hold."""
+    adj = _adj(problem)
+    Nn = problem["u"].shape[0]
+    g = torch.Generator(device=problem["u"].device).manual_seed(9)
+    B = torch.randn((Nn, 2, 8), generator=g, device=problem["u"].device, dtype=torch.float64)
+    B[~adj.active] = 0.0
+    X = adj.solve(B, rtol=1e-9)
+    for k in (0, 5):
+        Xk = adj.solve(B[:, :, k:k + 1].contiguous(), rtol=1e-9)
+        assert float((X[:, :, k] - Xk[:, :, 0]).abs().max()) <= 1e-6 * float(X[:, :, k].abs().max())
+    R = adj.matvec(X) - B
+    assert float(R[adj.active].norm()) <= 1e-5 * float(B.norm())
