@@ -55,7 +55,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-sample-frames", type=int, default=2)
-    p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--no-serve", action="store_true", help="skip the 512^2 small-frame serving stream")
+    p.add_argument("--serve-mixed", action="store_true", help="also run the reduced mixed serving stream")
     p.add_argument("--serve-seqs", type=int, default=16)
     p.add_argument("--serve-frames", type=int, default=4)
     p.add_argument("--serve-slots", type=int, default=32)
@@ -981,7 +982,8 @@ def run_ours(args, ws, rank, local):
     if not args.no_stream:
         out["serving_stream"] = run_serving_stream(args, dev)
     if not args.no_serve:
-        out["serving"] = run_serving(args, dev)
+        if args.serve_mixed:                       # the reduced mixed stream (the serving stream supersedes it)
+            out["serving"] = run_serving(args, dev)
         # the small-frame regime, where one frame alone cannot fill the GPU
         out["serving_small_frames"] = run_serving(args, dev, sides=(512,), n_seq=4 * args.serve_seqs,
                                                   label="small_frame_stream")
