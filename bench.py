@@ -603,7 +603,7 @@ def run_batched(args, dev):
 
     sides = tuple(int(x) for x in args.batch_sides.split(","))
     t0 = time.perf_counter()
-    wls = workloads.uneven_batch(args.batch_frames, device=dev, sides=sides)
+    wls = workloads.uneven_batch(args.batch_frames, device=dev, sides=sides, device_assets=True)
     t_assets = time.perf_counter() - t0
     tuner = default_tuner(dev)
     slots, shapes = [], []

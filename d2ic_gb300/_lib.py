@@ -23,6 +23,7 @@ MAX_ITERS = -4
 WAIT_TIMEOUT = -5
 CUDA_ERROR = -6
 UNSUPPORTED = -7
+INTERNAL = -8
 RUNNING = 1
 CMD_INIT, CMD_RUN, CMD_IDLE = 0, 1, 2
 STOP_ON_FINISH, STOP_ON_IRQ = 1, 2
@@ -37,7 +38,7 @@ TILE_MAX_FLOATS = 736
 
 STATUS_NAMES = {OK: "ok", BAD_ARG: "bad_arg", OOM: "oom", NAN_DETECTED: "nan_detected",
                 MAX_ITERS: "max_iters", WAIT_TIMEOUT: "wait_timeout", CUDA_ERROR: "cuda_error",
-                UNSUPPORTED: "unsupported", RUNNING: "running"}
+                UNSUPPORTED: "unsupported", INTERNAL: "internal", RUNNING: "running"}
 
 vp = ctypes.c_void_p
 i32 = ctypes.c_int

@@ -91,7 +91,9 @@ struct CtlHeader {
     int frames_done;        // frames whose control step ran in the current round
     int slice_stop;         // the slice ends after the released round (set before the release)
     int irq;                // written by the host while a slice runs: end the slice at the next round end
-    int pad_[3];
+    int list_buf;           // which of the two copies of the active list the current round reads
+    unsigned blocks_past;   // block arrivals at round ends: every block has finished a round's list reads
+    int pad_;
 };
 static_assert(sizeof(CtlHeader) == 64, "control header layout");
 
@@ -99,13 +101,23 @@ static_assert(sizeof(CtlHeader) == 64, "control header layout");
 enum { STOP_ON_FINISH = D2IC_STOP_ON_FINISH,   // after a round in which a frame finished
        STOP_ON_IRQ = D2IC_STOP_ON_IRQ };         // after a round that ends with the header's irq word set
 
+// The active list is double-buffered: a round reads copy h->list_buf while the warp that ends
+// the round may rebuild the list into the other copy (a frame finished) and flips list_buf before
+// the release.  Warps still walking the round's list -- lookups of padding groups, or the
+// rebuilding warp itself after the release -- therefore never see a half-written list.  Before it
+// writes, the rebuilding warp of round r waits until every block has passed the end of round r-1
+// (blocks_past), so no block still reads an older round's copy either.
 struct Ctl {
     CtlHeader *h;
     int *cmd;      // n_frames: CMD_INIT / CMD_RUN / CMD_IDLE
-    int *active;   // n_frames
-    int *cpre;     // n_frames + 1
-    int *gpre;     // n_frames + 1
+    int *active;   // two copies of n_frames
+    int *cpre;     // two copies of n_frames + 1
+    int *gpre;     // two copies of n_frames + 1
     FrameState *fs;
+    int n;         // n_frames
+    __device__ __forceinline__ int *act(int b) const { return active + b * n; }
+    __device__ __forceinline__ int *cp(int b) const { return cpre + b * (n + 1); }
+    __device__ __forceinline__ int *gp(int b) const { return gpre + b * (n + 1); }
 };
 
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -114,12 +126,12 @@ __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~(size
 __host__ __device__ inline size_t ctl_layout(int n, size_t *o_active, size_t *o_cpre, size_t *o_gpre, size_t *o_fs) {
     size_t off = align256(sizeof(CtlHeader));
     off = align256(off + sizeof(int) * (size_t)n);          // cmd
-    *o_active = off;
-    off = align256(off + sizeof(int) * (size_t)n);
+    *o_active = off;                                        // two copies of each list array
+    off = align256(off + 2 * sizeof(int) * (size_t)n);
     *o_cpre = off;
-    off = align256(off + sizeof(int) * (size_t)(n + 1));
+    off = align256(off + 2 * sizeof(int) * (size_t)(n + 1));
     *o_gpre = off;
-    off = align256(off + sizeof(int) * (size_t)(n + 1));
+    off = align256(off + 2 * sizeof(int) * (size_t)(n + 1));
     *o_fs = off;
     off = align256(off + sizeof(FrameState) * (size_t)n);
     return off;
@@ -134,6 +146,7 @@ __device__ inline Ctl make_ctl(char *base, int n) {
     c.active = (int *)(base + oa);
     c.cpre = (int *)(base + oc);
     c.gpre = (int *)(base + og);
+    c.n = n;
     c.fs = (FrameState *)(base + of);
     return c;
 }
@@ -296,6 +309,16 @@ __device__ __forceinline__ int find_slot_smem(const int *pre, int n, int x) {
         else hi = mid - 1;
     }
     return lo;
+}
+
+// Self-check of an index taken from the active list or its prefix sums: in [0, n) it is returned;
+// otherwise the launch aborts with D2IC_INTERNAL and 0 is returned, so that the access it guards
+// stays inside its table.
+__device__ __forceinline__ int checked_index(int v, int n, CtlHeader *H) {
+    if ((unsigned)v < (unsigned)n) return v;
+    H->err = D2IC_INTERNAL;
+    atomicExch(&H->abort, 1);
+    return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -843,19 +866,20 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
         }
     int ta, tb, tc;
     block_scan3(cnt, ch, gr, ta, tb, tc);
+    const int lb = ld_vol(&C.h->list_buf);         // start of a launch: nothing reads the list yet
     if (threadIdx.x == 0) {
         C.h->n_active = ta;
         C.h->total_chunks = tb;
         C.h->total_groups = tc;
-        C.cpre[ta] = tb;
-        C.gpre[ta] = tc;
+        C.cp(lb)[ta] = tb;
+        C.gp(lb)[ta] = tc;
     }
     int slot = cnt, cp = ch, gp = gr;
     for (int f = f0; f < f1; ++f)
         if (ld_vol(&C.fs[f].state) != ST_DONE) {
-            C.active[slot] = f;
-            C.cpre[slot] = cp;
-            C.gpre[slot] = gp;
+            C.act(lb)[slot] = f;
+            C.cp(lb)[slot] = cp;
+            C.gp(lb)[slot] = gp;
             ++slot;
             cp += frames[f].n_chunks;
             gp += pad_groups(frames[f].n_groups);
@@ -893,6 +917,23 @@ __device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
     rebuild_active(frames, n_frames, C);
 }
 
+// Wait (bounded) until blocks_past reaches target; on a timeout the launch aborts and the list
+// is left as it is.
+__device__ __forceinline__ int wait_blocks_past(CtlHeader *H, unsigned target) {
+    if (ld_acquire_u32(&H->blocks_past) >= target) return 1;
+    const unsigned long long t0 = gtimer();
+    while (ld_acquire_u32(&H->blocks_past) < target) {
+        if (ld_vol(&H->abort)) return 0;
+        if (gtimer() - t0 > WAIT_NS) {
+            H->err = D2IC_WAIT_TIMEOUT;
+            atomicExch(&H->abort, 1);
+            return 0;
+        }
+        __nanosleep(32);
+    }
+    return 1;
+}
+
 // The CG control of one frame, run by the warp that reduced the frame's last
 // node group: the group partials are summed in group order (double-float,
 // then FP64) and the frame state advanced.  Nothing else reads the frame's
@@ -922,12 +963,14 @@ __device__ void rebuild_active_warp(const d2ic_frame_t *frames, int n_frames, Ct
     }
     const int ta = __shfl_sync(0xffffffffu, ic, 31), tb = __shfl_sync(0xffffffffu, ih, 31),
               tc = __shfl_sync(0xffffffffu, ig, 31);
+    // the copy no block reads (see Ctl); read once, before lane 0 flips it below
+    const int nb = 1 - __shfl_sync(0xffffffffu, lane == 0 ? ld_vol(&C.h->list_buf) : 0, 0);
     int slot = ic - cnt, cp = ih - ch, gp = ig - gr;
     for (int f = f0; f < f1; ++f)
         if (ld_vol(&C.fs[f].state) != ST_DONE) {
-            C.active[slot] = f;
-            C.cpre[slot] = cp;
-            C.gpre[slot] = gp;
+            C.act(nb)[slot] = f;
+            C.cp(nb)[slot] = cp;
+            C.gp(nb)[slot] = gp;
             ++slot;
             cp += frames[f].n_chunks;
             gp += pad_groups(frames[f].n_groups);
@@ -936,8 +979,9 @@ __device__ void rebuild_active_warp(const d2ic_frame_t *frames, int n_frames, Ct
         C.h->n_active = ta;
         C.h->total_chunks = tb;
         C.h->total_groups = tc;
-        C.cpre[ta] = tb;
-        C.gpre[ta] = tc;
+        C.cp(nb)[ta] = tb;
+        C.gp(nb)[ta] = tc;
+        C.h->list_buf = nb;                          // published by the round's release
     }
     __syncwarp();
 }
@@ -990,14 +1034,14 @@ __device__ void frame_r(const d2ic_frame_t &F, int f, Ctl &C, int eval_only, int
 
 // The active list (n_active = na <= FCACHE) with its prefix sums and each frame's candidate
 // rule, copied into the block's shared memory (whole block).
-__device__ void load_list(Ctl &C, int na, int *s_cpre, int *s_gpre, int *s_act, FInfo *s_fi) {
+__device__ void load_list(Ctl &C, int lb, int na, int *s_cpre, int *s_gpre, int *s_act, FInfo *s_fi) {
     if (na > FCACHE) return;
     for (int s = threadIdx.x; s <= na; s += NT) {
-        s_cpre[s] = __ldcg(C.cpre + s);
-        s_gpre[s] = __ldcg(C.gpre + s);
+        s_cpre[s] = __ldcg(C.cp(lb) + s);
+        s_gpre[s] = __ldcg(C.gp(lb) + s);
     }
     for (int s = threadIdx.x; s < na; s += NT) {
-        const int f = __ldcg(C.active + s);
+        const int f = checked_index(__ldcg(C.act(lb) + s), C.n, C.h);
         s_act[s] = f;
         s_fi[s] = frame_info(C.fs + f);
     }
@@ -1022,7 +1066,8 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
     __shared__ int s_gpre[FCACHE + 1];
     __shared__ int s_act[FCACHE];
     __shared__ FInfo s_fi[FCACHE];
-    __shared__ int s_hdr[5];                         // n_active, total_chunks, total_groups, abort, slice_stop
+    __shared__ int s_hdr[6];                         // n_active, total_chunks, total_groups, abort, slice_stop,
+                                                     // list_buf
     __shared__ DF s_gq[NWARP][D2IC_NPART];           // group partials of this block's supergroup
     __shared__ int s_sgcnt;                          // groups of this block's supergroup reduced this round
     // per warp: two record buffers, then two coefficient-tile buffers (all 128-byte aligned)
@@ -1099,15 +1144,17 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         s_hdr[2] = ld_vol(&C.h->total_groups);
         s_hdr[3] = ld_vol(&C.h->abort);
         s_hdr[4] = 0;
+        s_hdr[5] = ld_vol(&C.h->list_buf);
     }
     __syncthreads();
-    load_list(C, s_hdr[0], s_cpre, s_gpre, s_act, s_fi);
+    load_list(C, s_hdr[5], s_hdr[0], s_cpre, s_gpre, s_act, s_fi);
     __syncthreads();
 
     while (round < max_rounds) {                    // a slice: at most max_rounds rounds, state kept in HBM
         const int na = s_hdr[0];
         const int total = s_hdr[1];
         const int tg = s_hdr[2];
+        const int lb = s_hdr[5];
         if (na == 0 || s_hdr[3] || s_hdr[4]) break;
         const bool trr = tr && round < trace_rounds;
         if (trr) trace[7 * round + 0] = gtimer();
@@ -1141,11 +1188,11 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                     f = s_act[s];
                     base = s_cpre[s];
                 } else {
-                    s = find_slot(C.cpre, na, g);
-                    f = __ldcg(C.active + s);
-                    base = __ldcg(C.cpre + s);
+                    s = find_slot(C.cp(lb), na, g);
+                    f = checked_index(__ldcg(C.act(lb) + s), n_frames, C.h);
+                    base = __ldcg(C.cp(lb) + s);
                 }
-                ChunkMeta m = load_meta(frames, f, g - base, lane);
+                ChunkMeta m = load_meta(frames, f, checked_index(g - base, frames[f].n_chunks, C.h), lane);
                 m.s = s;
                 return m;
             };
@@ -1278,12 +1325,13 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                             f = s_act[sl];
                             base = s_cpre[sl];
                         } else {
-                            const int sl = find_slot(C.cpre, na, g);
-                            f = __ldcg(C.active + sl);
-                            base = __ldcg(C.cpre + sl);
+                            const int sl = find_slot(C.cp(lb), na, g);
+                            f = checked_index(__ldcg(C.act(lb) + sl), n_frames, C.h);
+                            base = __ldcg(C.cp(lb) + sl);
                         }
                         const d2ic_frame_t &F = frames[f];
-                        grp = __ldg(F.chunk_nodes + 4 * (g - base) + (lane & 3)) / GN;
+                        const int c = checked_index(g - base, F.n_chunks, C.h);
+                        grp = __ldg(F.chunk_nodes + 4 * c + (lane & 3)) / GN;
                         cnt = F.group_cnt;
                     }
                     count_chunk_groups_quad(cnt, grp, lane);
@@ -1304,13 +1352,17 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                     f = s_act[s];
                     base = s_gpre[s];
                 } else {
-                    s = find_slot(C.gpre, na, gi);
-                    f = __ldcg(C.active + s);
-                    base = __ldcg(C.gpre + s);
+                    s = find_slot(C.gp(lb), na, gi);
+                    f = checked_index(__ldcg(C.act(lb) + s), n_frames, C.h);
+                    base = __ldcg(C.gp(lb) + s);
                 }
                 const d2ic_frame_t &F = frames[f];
                 const int g = gi - base;
                 if (g >= F.n_groups) continue;         // padding of the frame's group range
+                if (g < 0) {                           // self-check: the prefix sums are ascending
+                    checked_index(g, 0, C.h);
+                    continue;
+                }
                 const FInfo fi = cached ? s_fi[s] : frame_info(C.fs + f);
                 const NodePre pre = node_pre(F, fi, g * GN + lane);   // independent of the pixel pass
                 int ok = 1;
@@ -1404,7 +1456,11 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
                             if (lane == 0) C.h->frames_done = 0;
                             int stop = 0;
                             if (ld_vol(&C.h->finished)) {
-                                rebuild_active_warp(frames, n_frames, C, lane);
+                                // no block still reads the list copy of an earlier round (bounded)
+                                int past = 1;
+                                if (lane == 0) past = wait_blocks_past(C.h, gridDim.x * (unsigned)round);
+                                if (__shfl_sync(0xffffffffu, past, 0))
+                                    rebuild_active_warp(frames, n_frames, C, lane);
                                 if (lane == 0) C.h->finished = 0;
                                 stop = stop_flags & STOP_ON_FINISH;
                             }
@@ -1437,6 +1493,7 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
         // (rounds_done is monotonic, so a block that arrives after the release passes at once) ----
         __syncthreads();
         if (threadIdx.x == 0) {
+            atomicAdd(&C.h->blocks_past, 1u);           // this block's list reads of the round are done
             const unsigned target = (unsigned)(round + 1);
             if (ld_acquire_u32(&C.h->rounds_done) < target) {
                 const unsigned long long t0 = gtimer();
@@ -1461,12 +1518,13 @@ __global__ void __launch_bounds__(NT, D2IC_ENGINE_MINB) cg_engine(const d2ic_fra
             s_hdr[2] = ld_vol(&C.h->total_groups);
             s_hdr[3] = ld_vol(&C.h->abort);
             s_hdr[4] = ld_vol(&C.h->slice_stop);
+            s_hdr[5] = ld_vol(&C.h->list_buf);
         }
         if (na <= FCACHE)
             for (int s = threadIdx.x; s < na; s += NT) s_fi[s] = frame_info(C.fs + s_act[s]);
         __syncthreads();
         if (s_hdr[0] != na && s_hdr[0] > 0 && !s_hdr[3]) {
-            load_list(C, s_hdr[0], s_cpre, s_gpre, s_act, s_fi);
+            load_list(C, s_hdr[5], s_hdr[0], s_cpre, s_gpre, s_act, s_fi);
             __syncthreads();
         }
         if (trr) trace[7 * round + 5] = gtimer();

@@ -192,19 +192,14 @@ def serving_stream(n_arrivals: int = 4096, n_seq: int = 128, seed: int = 4, devi
             frames.append(h)
         ref = ref_d.cpu().numpy()
         specs.append((s, H, elem[s], ref, frames, ellipse_mask(H, H, r), warps))
-    built = None
     if device_assets:
-        try:
-            from .pixel_assets import build_pixel_assets_device
-        except ImportError:
-            build_pixel_assets_device = None
-        if build_pixel_assets_device is not None:
-            built = []
-            for sp in specs:
-                mesh, assets = mask_to_mesh_assets(sp[5], sp[2])
-                built.append((mesh, replace(assets, pixel_data=build_pixel_assets_device(mesh, sp[3], 1.0,
-                                                                                          assets.roi_mask))))
-    if built is None:
+        from .pixel_assets import build_pixel_assets_device
+        built = []
+        for sp in specs:
+            mesh, assets = mask_to_mesh_assets(sp[5], sp[2])
+            built.append((mesh, replace(assets, pixel_data=build_pixel_assets_device(mesh, sp[3], 1.0,
+                                                                                      assets.roi_mask))))
+    else:
         built = _build_assets([(sp[5], sp[3].astype(np.float32)) for sp in specs], [sp[2] for sp in specs])
     seqs = [StreamSequence(s, H, e, ref, mesh, assets, frames,
                            MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1),
@@ -229,17 +224,19 @@ def plate_hole_2048(n_frames: int = 20, seed: int = 1, device="cpu", H: int = 20
 
 
 def uneven_batch(n_frames: int = 64, seed: int = 2, device="cpu", sides=(512, 1024, 2048, 3072, 4096),
-                 elements=(8, 12, 16, 24, 32)):
+                 elements=(8, 12, 16, 24, 32), device_assets: bool = False):
     """Independent frames of uneven size for one batched launch (frame i uses seed ``2000 + i``).
 
     Per frame: side and element size drawn uniformly, ellipse mask covering
     40-90%, a random affine map (strains +-2%, rotation +-1 deg, translation
     +-3 px) about the image centre, N(0, 0.5^2) grey noise on both images.
+    ``device_assets``: images rendered on the device (float32, the device noise generator) and
+    pixel assets as device-layout recipes (build_pixel_assets_device) instead of host arrays.
     """
     import math
     from dataclasses import replace
 
-    from .synthetic import Affine, ellipse_mask
+    from .synthetic import Affine, ellipse_mask, speckle_sequence_device
     rng = np.random.default_rng(seed)
     specs = []
     for i in range(n_frames):
@@ -252,10 +249,24 @@ def uneven_batch(n_frames: int = 64, seed: int = 2, device="cpu", sides=(512, 10
         A = np.array([[exx, exy], [exy, eyy]]) + np.array([[math.cos(th) - 1, -math.sin(th)],
                                                           [math.sin(th), math.cos(th) - 1]])
         warp = Affine(A, t, [H / 2, H / 2])
-        ref, frames = speckle_sequence(H, H, [warp], seed=2000 + i, noise_seeds=[20000 + 2 * i, 20001 + 2 * i],
-                                       noise_sigma=0.5, device=device)
+        if device_assets:
+            ref_d, frames = speckle_sequence_device(H, H, [warp], seed=2000 + i,
+                                                    noise_seeds=[20000 + 2 * i, 20001 + 2 * i],
+                                                    noise_sigma=0.5, device=device, u8=False)
+            ref = ref_d.cpu().numpy()
+        else:
+            ref, frames = speckle_sequence(H, H, [warp], seed=2000 + i, noise_seeds=[20000 + 2 * i, 20001 + 2 * i],
+                                           noise_sigma=0.5, device=device)
         specs.append((i, H, elem, ref, frames, ellipse_mask(H, H, r), warp))
-    built = _build_assets([(sp[5], sp[3]) for sp in specs], [sp[2] for sp in specs])
+    if device_assets:
+        from .pixel_assets import build_pixel_assets_device
+        built = []
+        for sp in specs:
+            mesh, assets = mask_to_mesh_assets(sp[5], sp[2])
+            built.append((mesh, replace(assets, pixel_data=build_pixel_assets_device(mesh, sp[3], 1.0,
+                                                                                      assets.roi_mask))))
+    else:
+        built = _build_assets([(sp[5], sp[3]) for sp in specs], [sp[2] for sp in specs])
     return [Workload(f"frame{i}_{H}px_e{elem}", ref, frames, mask, mesh, assets,
                      MeshDICConfig(max_iters=200, tol=1e-3, reg_strength=0.1), None, [warp])
             for (i, H, elem, ref, frames, mask, warp), (mesh, assets) in zip(specs, built)]

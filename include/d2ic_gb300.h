@@ -37,6 +37,7 @@ extern "C" {
 #define D2IC_WAIT_TIMEOUT  -5   /* a bounded device-side wait gave up         */
 #define D2IC_CUDA_ERROR    -6
 #define D2IC_UNSUPPORTED   -7
+#define D2IC_INTERNAL      -8   /* an engine self-check failed (an index outside its table) */
 #define D2IC_RUNNING        1   /* per-frame status: not finished at the end of a slice */
 
 /* interpolation kinds (GlobalCGSolver(interpolation=...)) */

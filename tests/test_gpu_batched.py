@@ -213,3 +213,31 @@ def test_slice_stops_when_a_frame_finishes(cuda, uneven):
     for s, o in zip(slots, one):
         assert int(s.info[0]) == o[1]
         assert np.array_equal(s.u_out.cpu().numpy(), o[0])
+
+
+def test_batch_beyond_the_shared_list_equals_alone(cuda):
+    """More active frames than the engine keeps in shared memory (64): the rounds then look the
+    active list up in HBM, and frames that finish in different rounds rebuild it while other
+    warps still walk it.  Every frame must still be bitwise its solve alone."""
+    import d2ic_gb300 as d2
+    from d2ic_gb300 import engine
+    from d2ic_gb300.serving import solve_batch
+    from d2ic_gb300.synthetic import Translation, rect_mask, speckle_sequence
+    items = []
+    for k, (H, elem) in enumerate([(96, 12), (112, 16), (128, 12), (96, 16)]):
+        warps = [Translation(0.05 * j - 0.4, 0.3 - 0.03 * j) for j in range(21)]
+        ref, frames = speckle_sequence(H, H, warps, seed=50 + k, noise_seeds=list(range(60, 82)))
+        mesh, assets = d2.mask_to_mesh_assets(rect_mask(H, H, H - 16, H - 16), elem)
+        pix = d2.build_pixel_assets(mesh, ref, 1.0, assets.roi_mask)
+        L = engine.FrameLayout(pix, mesh.nodes_xy.shape[0], ref, "cubic", cuda)
+        for j, img in enumerate(frames):
+            # caps from 12 to 60 iterations: frames leave the list in many different rounds
+            cfg = d2.MeshDICConfig(max_iters=12 + 2 * ((7 * j + 5 * k) % 25), tol=1e-5, reg_strength=0.1)
+            items.append((L, img, None, cfg))
+    assert len(items) == 84
+    mixed = solve_batch(items, cuda)
+    for it, m in zip(items, mixed):
+        a = solve_batch([it], cuda)[0]
+        assert a[1] == m[1] and a[2] == m[2]
+        assert np.array_equal(a[0], m[0])                      # bitwise
+        assert np.array_equal(a[3], m[3], equal_nan=True)
