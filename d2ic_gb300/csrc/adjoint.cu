@@ -238,50 +238,72 @@ __global__ void hv_nodes(const d2ic_frame_t *__restrict__ fp, const float *__res
     Y[((size_t)n * 2 + 1) * K + k] = sy * inv_np + alpha * ry;
 }
 
-// (d grad_u J / dI2) dI, per chunk into node slots (float2 per node, plane `slot`)
+// (d grad_u J / dI2) dI for the images of a batch, one block per chunk: its pixels are located and
+// sampled in the frame once (position, residual r, gradient g; one pixel per thread, kept in shared
+// memory), then warp w takes images w, w + 8, ...: per pixel dv and grad dv of the image's
+// coefficients at the same position, t = dv g + r grad dv, and the chunk's node sums N_a t (lane
+// order, then a warp sum) into the image's node slots.  The frame sample is shared by all images
+// of the batch instead of being repeated per image.
 __global__ void __launch_bounds__(256) mixed_chunks(const d2ic_frame_t *__restrict__ fp, const float2 *__restrict__ u,
                                                     const float *__restrict__ dcoeff, float2 *__restrict__ slots,
-                                                    size_t coeff_stride, size_t slot_stride) {
+                                                    size_t coeff_stride, size_t slot_stride, int n_images) {
+    __shared__ int s_ix[D2IC_CHUNK_MAX], s_iy[D2IC_CHUNK_MAX];
+    __shared__ float s_tx[D2IC_CHUNK_MAX], s_ty[D2IC_CHUNK_MAX];
+    __shared__ float s_r[D2IC_CHUNK_MAX], s_gx[D2IC_CHUNK_MAX], s_gy[D2IC_CHUNK_MAX];
+    __shared__ float s_N[4][D2IC_CHUNK_MAX];
     const d2ic_frame_t &F = *fp;
-    dcoeff += blockIdx.y * coeff_stride;               // image blockIdx.y of a batch
-    slots += blockIdx.y * slot_stride;
-    const int lane = threadIdx.x & 31;
-    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (c >= F.n_chunks) return;
+    const int c = blockIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     float ux[4], uy[4];
     int nd, slot;
     chunk_nodes_u(F, u, c, lane, ux, uy, nd, slot);
-    const Img im{F.coeff, F.W, F.H, F.cpitch, F.pad};
-    const Img dm{dcoeff, F.W, F.H, F.cpitch, F.pad};
-    float ax[4] = {0.f, 0.f, 0.f, 0.f}, ay[4] = {0.f, 0.f, 0.f, 0.f};
-    const int pb = __ldg(F.chunk_begin + c), pe = __ldg(F.chunk_begin + c + 1);
-    for (int p = pb + lane; p < pe; p += 32) {
-        const ChunkPix q = unpack(__ldg(reinterpret_cast<const uint4 *>(F.pix) + p));
+    const int pb = __ldg(F.chunk_begin + c), n = min(__ldg(F.chunk_begin + c + 1) - pb, D2IC_CHUNK_MAX);
+    if ((int)threadIdx.x < n) {
+        const int i = threadIdx.x;
+        const ChunkPix q = unpack(__ldg(reinterpret_cast<const uint4 *>(F.pix) + pb + i));
         const float dx = q.N[0] * ux[0] + q.N[1] * ux[1] + q.N[2] * ux[2] + q.N[3] * ux[3];
         const float dy = q.N[0] * uy[0] + q.N[1] * uy[1] + q.N[2] * uy[2] + q.N[3] * uy[3];
         int ix, iy;
         float tx, ty;
         split_coord(q.x, dx, ix, tx);
         split_coord(q.y, dy, iy, ty);
-        float gx, gy, dgx, dgy;
-        const float r = sample_cubic(im, ix, iy, tx, ty, gx, gy) - q.I1;
-        const float dv = sample_cubic(dm, ix, iy, tx, ty, dgx, dgy);
-        const float txv = dv * gx + r * dgx, tyv = dv * gy + r * dgy;
+        const Img im{F.coeff, F.W, F.H, F.cpitch, F.pad};
+        float gx, gy;
+        s_r[i] = sample_cubic(im, ix, iy, tx, ty, gx, gy) - q.I1;
+        s_gx[i] = gx;
+        s_gy[i] = gy;
+        s_ix[i] = ix;
+        s_iy[i] = iy;
+        s_tx[i] = tx;
+        s_ty[i] = ty;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) s_N[a][i] = q.N[a];
+    }
+    __syncthreads();
+    for (int b = w; b < n_images; b += 8) {
+        const Img dm{dcoeff + (size_t)b * coeff_stride, F.W, F.H, F.cpitch, F.pad};
+        float ax[4] = {0.f, 0.f, 0.f, 0.f}, ay[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int i = lane; i < n; i += 32) {
+            float dgx, dgy;
+            const float dv = sample_cubic(dm, s_ix[i], s_iy[i], s_tx[i], s_ty[i], dgx, dgy);
+            const float r = s_r[i];
+            const float txv = dv * s_gx[i] + r * dgx, tyv = dv * s_gy[i] + r * dgy;
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                ax[a] += s_N[a][i] * txv;
+                ay[a] += s_N[a][i] * tyv;
+            }
+        }
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-            ax[a] += q.N[a] * txv;
-            ay[a] += q.N[a] * tyv;
+            ax[a] = warp_sum_f(ax[a]);
+            ay[a] = warp_sum_f(ay[a]);
         }
-    }
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        ax[a] = warp_sum_f(ax[a]);
-        ay[a] = warp_sum_f(ay[a]);
-    }
-    if (lane < 4) {
-        const float gx = lane == 0 ? ax[0] : lane == 1 ? ax[1] : lane == 2 ? ax[2] : ax[3];
-        const float gy = lane == 0 ? ay[0] : lane == 1 ? ay[1] : lane == 2 ? ay[2] : ay[3];
-        slots[(size_t)slot * F.n_nodes + nd] = make_float2(gx, gy);
+        if (lane < 4) {
+            const float gx = lane == 0 ? ax[0] : lane == 1 ? ax[1] : lane == 2 ? ax[2] : ax[3];
+            const float gy = lane == 0 ? ay[0] : lane == 1 ? ay[1] : lane == 2 ? ay[2] : ay[3];
+            slots[(size_t)b * slot_stride + (size_t)slot * F.n_nodes + nd] = make_float2(gx, gy);
+        }
     }
 }
 
@@ -417,8 +439,7 @@ extern "C" int d2ic_mixed_term(const d2ic_frame_t *frame_dev, int n_chunks, int 
                  "d2ic_mixed_term: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
     if (n_chunks > 0) {
-        mixed_chunks<<<(n_chunks * 32 + 255) / 256, 256, 0, s>>>(frame_dev, (const float2 *)u, dcoeff, (float2 *)slots,
-                                                                 0, 0);
+        mixed_chunks<<<n_chunks, 256, 0, s>>>(frame_dev, (const float2 *)u, dcoeff, (float2 *)slots, 0, 0, 1);
         D2IC_CHECK_LAUNCH("mixed_chunks");
     }
     slots_to_nodes<<<(n_nodes + 255) / 256, 256, 0, s>>>(frame_dev, (const float2 *)slots, scale, out, K, k, 0);
@@ -435,8 +456,8 @@ extern "C" int d2ic_mixed_term_batch(const d2ic_frame_t *frame_dev, int n_chunks
     cudaStream_t s = (cudaStream_t)stream;
     const size_t slot_stride = (size_t)node_chunk_k * n_nodes;   // float2 per image
     if (n_chunks > 0) {
-        mixed_chunks<<<dim3((n_chunks * 32 + 255) / 256, n_images), 256, 0, s>>>(
-            frame_dev, (const float2 *)u, dcoeff, (float2 *)slots, (size_t)coeff_stride, slot_stride);
+        mixed_chunks<<<n_chunks, 256, 0, s>>>(frame_dev, (const float2 *)u, dcoeff, (float2 *)slots,
+                                              (size_t)coeff_stride, slot_stride, n_images);
         D2IC_CHECK_LAUNCH("mixed_chunks");
     }
     slots_to_nodes<<<dim3((n_nodes + 255) / 256, n_images), 256, 0, s>>>(frame_dev, (const float2 *)slots, scale, out,

@@ -34,32 +34,55 @@ static int ensure_fir() {
 }
 
 // rows: tmp[y][cx] = sum_k h[k] img[y][clamp(cx - pad + k)], cx in [0, W + 2 pad); image
-// blockIdx.z of a batch (contiguous images and buffers).  T: float or 8-bit camera pixels.
+// blockIdx.z of a batch (contiguous images and buffers).  T: float or 8-bit camera pixels.  A block
+// takes an even share (at most RT_OUT outputs, a multiple of 4) of one row, its edge-extended
+// segment staged once in shared memory; a thread makes 4 consecutive outputs from 10 float4 reads
+// of the segment (each output's taps still summed in order k = 0 .. 2 KF).  The host sizes the
+// block to the share (rows_launch), so that no warp idles on 1024- or 2048-pixel rows.
+constexpr int RT_OUT = 4096;
 template <class T>
-__global__ void __launch_bounds__(256) prefilter_rows(const T *__restrict__ img, int H, int W, int pad,
+__global__ void __launch_bounds__(1024) prefilter_rows(const T *__restrict__ img, int H, int W, int pad,
                                                       int cpitch, float *__restrict__ tmp) {
-    __shared__ float s[256 + 2 * KF];
+    __shared__ __align__(16) float s[RT_OUT + 2 * KF + 4];
     img += (size_t)blockIdx.z * H * W;
     tmp += (size_t)blockIdx.z * H * cpitch;
     const int y = blockIdx.y;
-    const int cx0 = blockIdx.x * 256;
+    const int CW = W + 2 * pad;
+    const int per = (((CW + gridDim.x - 1) / gridDim.x) + 3) & ~3;   // <= RT_OUT
+    const int cx0 = blockIdx.x * per;
+    const int n_out = min(per, CW - cx0);
     const T *row = img + (size_t)y * W;
-    for (int i = threadIdx.x; i < 256 + 2 * KF; i += 256) {
+    for (int i = threadIdx.x; i < ((n_out + 3) & ~3) + 2 * KF + 4; i += blockDim.x) {
         const int src = clampi(cx0 - pad - KF + i, 0, W - 1);
         s[i] = (float)__ldg(row + src);
     }
     __syncthreads();
-    const int cx = cx0 + threadIdx.x;
-    if (cx < W + 2 * pad) {
-        float acc = 0.f;
+    const int o0 = 4 * threadIdx.x;
+    if (o0 >= n_out) return;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    const float4 *s4 = reinterpret_cast<const float4 *>(s) + threadIdx.x;
 #pragma unroll
-        for (int k = 0; k <= 2 * KF; ++k) acc += c_fir[k] * s[threadIdx.x + k];
-        tmp[(size_t)y * cpitch + cx] = acc;
+    for (int m = 0; m < (2 * KF + 4) / 4 + 1; ++m) {
+        const float4 q = s4[m];
+        const float v[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                const int k = 4 * m + e - o;
+                if (k >= 0 && k <= 2 * KF) acc[o] += c_fir[k] * v[e];
+            }
     }
+    float *out = tmp + (size_t)y * cpitch + cx0 + o0;
+#pragma unroll
+    for (int o = 0; o < 4; ++o)
+        if (o0 + o < n_out) out[o] = acc[o];
 }
 
-// columns: coeff[cy][cx] = sum_k h[k] tmp[clamp(cy - pad + k)][cx], cy in [0, H + 2 pad)
-constexpr int CT_W = 32, CT_H = 64;
+// columns: coeff[cy][cx] = sum_k h[k] tmp[clamp(cy - pad + k)][cx], cy in [0, H + 2 pad).  A block
+// takes CT_W columns x CT_H rows; thread (x, y) makes the CT_R consecutive rows y CT_R .. of column x
+// from CT_R + 2 KF shared-memory reads (sliding window, taps in order k = 0 .. 2 KF per output).
+constexpr int CT_W = 32, CT_H = 128, CT_R = CT_H / 8;
 __global__ void __launch_bounds__(256) prefilter_cols(const float *__restrict__ tmp, int H, int W, int pad,
                                                       int cpitch, float *__restrict__ coeff) {
     __shared__ float s[CT_H + 2 * KF][CT_W + 1];
@@ -74,14 +97,36 @@ __global__ void __launch_bounds__(256) prefilter_cols(const float *__restrict__ 
     }
     __syncthreads();
     if (cx >= CW) return;
-    for (int r = threadIdx.y; r < CT_H; r += 8) {
-        const int cy = cy0 + r;
-        if (cy >= H + 2 * pad) break;
-        float acc = 0.f;
+    const int r0 = threadIdx.y * CT_R;
+    float acc[CT_R];
 #pragma unroll
-        for (int k = 0; k <= 2 * KF; ++k) acc += c_fir[k] * s[r + k][threadIdx.x];
-        coeff[(size_t)cy * cpitch + cx] = acc;
+    for (int o = 0; o < CT_R; ++o) acc[o] = 0.f;
+#pragma unroll
+    for (int j = 0; j < CT_R + 2 * KF; ++j) {
+        const float v = s[r0 + j][threadIdx.x];
+#pragma unroll
+        for (int o = 0; o < CT_R; ++o) {
+            const int k = j - o;
+            if (k >= 0 && k <= 2 * KF) acc[o] += c_fir[k] * v;
+        }
     }
+#pragma unroll
+    for (int o = 0; o < CT_R; ++o) {
+        const int cy = cy0 + r0 + o;
+        if (cy < H + 2 * pad) coeff[(size_t)cy * cpitch + cx] = acc[o];
+    }
+}
+
+// blocks per row and threads per block of prefilter_rows for rows of CW outputs: the fewest blocks
+// of at most RT_OUT outputs, and one thread per 4 outputs of the (even, 4-aligned) share
+struct RowsLaunch {
+    unsigned blocks, threads;
+};
+static RowsLaunch rows_launch(int CW) {
+    const int blocks = (CW + RT_OUT - 1) / RT_OUT;
+    const int per = (((CW + blocks - 1) / blocks) + 3) & ~3;
+    const int quads = per / 4;
+    return RowsLaunch{(unsigned)blocks, (unsigned)(((quads + 31) / 32) * 32)};
 }
 
 template <class T>
@@ -103,7 +148,8 @@ static int prefilter_one(const T *img, int H, int W, int pad, int cpitch, float 
     int st = ensure_fir();
     if (st) return st;
     const int CW = W + 2 * pad;
-    prefilter_rows<T><<<dim3((CW + 255) / 256, H), 256, 0, s>>>(img, H, W, pad, cpitch, tmp);
+    const RowsLaunch rl = rows_launch(CW);
+    prefilter_rows<T><<<dim3(rl.blocks, H), rl.threads, 0, s>>>(img, H, W, pad, cpitch, tmp);
     D2IC_CHECK_LAUNCH("prefilter_rows");
     prefilter_cols<<<dim3((CW + CT_W - 1) / CT_W, (H + 2 * pad + CT_H - 1) / CT_H), dim3(CT_W, 8), 0, s>>>(
         tmp, H, W, pad, cpitch, coeff);
@@ -164,7 +210,8 @@ extern "C" int d2ic_bspline_prefilter_batch(const float *img, int n_images, int 
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
     const int CW = W + 2 * pad;
-    prefilter_rows<float><<<dim3((CW + 255) / 256, H, n_images), 256, 0, s>>>(img, H, W, pad, cpitch, tmp);
+    const RowsLaunch rl = rows_launch(CW);
+    prefilter_rows<float><<<dim3(rl.blocks, H, n_images), rl.threads, 0, s>>>(img, H, W, pad, cpitch, tmp);
     D2IC_CHECK_LAUNCH("prefilter_rows");
     prefilter_cols<<<dim3((CW + CT_W - 1) / CT_W, (H + 2 * pad + CT_H - 1) / CT_H, n_images), dim3(CT_W, 8), 0, s>>>(
         tmp, H, W, pad, cpitch, coeff);

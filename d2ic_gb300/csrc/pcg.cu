@@ -242,19 +242,51 @@ __device__ __forceinline__ void hop_row4(const HopTile &T, int w, int K, int k0,
     }
 }
 
-// Y = H V for K a multiple of 4: block = 8 nodes (warps) x 128 columns (4 per lane)
-__global__ void __launch_bounds__(256) hop_apply4(const int *__restrict__ idx, const float4 *__restrict__ blk,
-                                                  int n_nodes, const float *__restrict__ V, int K,
-                                                  float *__restrict__ Y) {
-    __shared__ HopTile T;
-    hop_stage(idx, blk, n_nodes, T);
+// Y = H V for K a multiple of 4: one warp per node (8 per block), lane l on columns 4 l .. 4 l + 3 of
+// each 128-column pass over K.  The node's entries are staged once per warp in shared memory (no
+// block-wide barrier) and read as broadcasts; per column the operations are those of hop_row.  At
+// 32 registers 64 warps fit on an SM, so a frame's nodes (one warp each) run in a single wave on
+// 152 SMs up to 9,728 nodes instead of queueing a second, mostly empty wave of blocks.
+__global__ void __launch_bounds__(256, 8) hop_apply4(const int *__restrict__ idx, const float4 *__restrict__ blk,
+                                                     int n_nodes, const float *__restrict__ V, int K,
+                                                     float *__restrict__ Y) {
+    __shared__ int s_j[8][HOP];
+    __shared__ float4 s_b[8][HOP];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int n = blockIdx.x * 8 + w, k0 = blockIdx.y * 128 + 4 * lane;
-    if (n >= n_nodes || k0 >= K) return;
-    float4 yx, yy;
-    hop_row4(T, w, K, k0, V, yx, yy);
-    *reinterpret_cast<float4 *>(Y + ((size_t)n * 2) * K + k0) = yx;
-    *reinterpret_cast<float4 *>(Y + ((size_t)n * 2 + 1) * K + k0) = yy;
+    const int n = blockIdx.x * 8 + w;
+    if (n >= n_nodes) return;                  // the whole warp: nothing below waits on the block
+    int j = -1;
+    if (lane < HOP) {
+        j = __ldg(idx + (size_t)n * HOP + lane);
+        s_j[w][lane] = j;
+        s_b[w][lane] = __ldg(blk + (size_t)n * HOP + lane);
+    }
+    const int cnt = __popc(__ballot_sync(0xffffffffu, j >= 0));   // entries are packed from the first
+    __syncwarp();
+    // float4 offsets within 32 bits (the host checks n_nodes * 2 * K < 2^31): row 2 j at j * K / 2
+    const int h = K >> 1, q4 = K >> 2;
+    const float4 *V4 = reinterpret_cast<const float4 *>(V);
+    float4 *Y4 = reinterpret_cast<float4 *>(Y) + n * h;
+    for (int c = lane; c < q4; c += 32) {
+        float4 yx = make_float4(0.f, 0.f, 0.f, 0.f), yy = yx;
+#pragma unroll 1
+        for (int q = 0; q < cnt; ++q) {
+            const int r = s_j[w][q] * h + c;
+            const float4 b = s_b[w][q];
+            const float4 vx = __ldg(V4 + r);
+            const float4 vy = __ldg(V4 + r + q4);
+            yx.x = __fmaf_rn(b.x, vx.x, __fmaf_rn(b.y, vy.x, yx.x));
+            yx.y = __fmaf_rn(b.x, vx.y, __fmaf_rn(b.y, vy.y, yx.y));
+            yx.z = __fmaf_rn(b.x, vx.z, __fmaf_rn(b.y, vy.z, yx.z));
+            yx.w = __fmaf_rn(b.x, vx.w, __fmaf_rn(b.y, vy.w, yx.w));
+            yy.x = __fmaf_rn(b.y, vx.x, __fmaf_rn(b.z, vy.x, yy.x));
+            yy.y = __fmaf_rn(b.y, vx.y, __fmaf_rn(b.z, vy.y, yy.y));
+            yy.z = __fmaf_rn(b.y, vx.z, __fmaf_rn(b.z, vy.z, yy.z));
+            yy.w = __fmaf_rn(b.y, vx.w, __fmaf_rn(b.z, vy.w, yy.w));
+        }
+        Y4[c] = yx;
+        Y4[c + q4] = yy;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -568,9 +600,10 @@ extern "C" int d2ic_hessian_apply(const void *op, int n_nodes, int node_chunk_k,
     D2IC_REQUIRE(op && V && Y && n_nodes >= 1 && K >= 1 && node_chunk_k >= 1, "d2ic_hessian_apply: bad arguments");
     HopView hv;
     hop_layout(n_nodes, node_chunk_k, (char *)op, &hv);
-    if (K % 4 == 0 && ((uintptr_t)V & 15) == 0 && ((uintptr_t)Y & 15) == 0) {
-        hop_apply4<<<dim3((unsigned)((n_nodes + 7) / 8), (unsigned)((K + 127) / 128)), 256, 0,
-                     (cudaStream_t)stream>>>(hv.idx, hv.blk, n_nodes, V, K, Y);
+    if (K % 4 == 0 && ((uintptr_t)V & 15) == 0 && ((uintptr_t)Y & 15) == 0 &&
+        (long long)n_nodes * 2 * K < (1ll << 31)) {
+        hop_apply4<<<(unsigned)((n_nodes + 7) / 8), 256, 0, (cudaStream_t)stream>>>(hv.idx, hv.blk, n_nodes, V, K,
+                                                                                      Y);
         D2IC_CHECK_LAUNCH("hop_apply4");
     } else {
         hop_apply<<<dim3((unsigned)((n_nodes + 7) / 8), (unsigned)((K + 31) / 32)), 256, 0, (cudaStream_t)stream>>>(
