@@ -715,6 +715,61 @@ def run_local(args, dev, wl, dic):
             "discrepancy_rms": rms, "discrepancy_ms": 1000 * (time.perf_counter() - t1) / 5}
 
 
+def run_init_motion(args, dev, wl):
+    """The first frame's initial motion: ZNCC integer search at the element centres and IDW onto the
+    nodes (kernels timed alone with CUDA events), on the workload's frame 0, plus IDW at the largest
+    mesh of the serving stream (4096^2 at 8 px: every grid node from every element centre)."""
+    import torch
+
+    from d2ic_gb300.dic_init_motion import project_centers_to_nodes_idw_device
+    from d2ic_gb300.solver_translation_zncc import match_centers_device
+
+    win, search = wl.init.win, wl.init.search
+    centers = torch.as_tensor(np.asarray(wl.assets.element_centers_xy, dtype=np.float32), device=dev).reshape(-1, 2)
+    ref = torch.as_tensor(wl.ref, device=dev)
+    img = torch.as_tensor(wl.frames[0], device=dev)
+    nodes = torch.as_tensor(np.asarray(wl.mesh.nodes_xy, dtype=np.float32), device=dev)
+
+    def timed(fn, reps=10):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    u_c, sc = match_centers_device(centers, ref, img, win, search, dev)
+    t_zncc = timed(lambda: match_centers_device(centers, ref, img, win, search, dev))
+    t_idw = timed(lambda: project_centers_to_nodes_idw_device(nodes, centers, u_c, 2.0, dev))
+    nc, nn = centers.shape[0], nodes.shape[0]
+    npx, npa = win * win, (2 * search + 1) ** 2
+    # FLOPs per offset: window sum (n adds), then per pixel centring (1), variance (2) and
+    # cross-correlation (2): 6 n
+    zflops = nc * npa * 6.0 * npx
+    fp32_nominal = 152 * 128 * 2 * 2.07                     # GFLOP/s: 152 SMs x 128 lanes x FMA x 2.07 GHz
+    # the serving stream's largest mesh: 4096^2 at 8 px, 513^2 nodes, 512^2 element centres
+    g = torch.arange(0, 4097, 8, dtype=torch.float32, device=dev)
+    big_nodes = torch.stack(torch.meshgrid(g, g, indexing="xy"), -1).reshape(-1, 2).contiguous()
+    gc = torch.arange(4, 4096, 8, dtype=torch.float32, device=dev)
+    big_centers = torch.stack(torch.meshgrid(gc, gc, indexing="xy"), -1).reshape(-1, 2).contiguous()
+    big_disp = torch.randn(big_centers.shape, generator=torch.Generator(device=dev).manual_seed(4),
+                           device=dev, dtype=torch.float32)
+    t_big = timed(lambda: project_centers_to_nodes_idw_device(big_nodes, big_centers, big_disp, 2.0, dev), reps=2)
+    pairs_big = big_nodes.shape[0] * big_centers.shape[0]
+    return {"workload": wl.name, "centres": int(nc), "nodes": int(nn), "win": win, "search": search,
+            "zncc_ms": t_zncc, "zncc_gflops": zflops / (t_zncc * 1e-3) / 1e9,
+            "zncc_frac_of_nominal_fp32": zflops / (t_zncc * 1e-3) / 1e9 / fp32_nominal,
+            "fp32_nominal_gflops": fp32_nominal, "idw_ms": t_idw,
+            "idw_pairs_per_s": nc * nn / (t_idw * 1e-3),
+            "idw_4096_e8": {"nodes": int(big_nodes.shape[0]), "centres": int(big_centers.shape[0]), "ms": t_big,
+                            "pairs_per_s": pairs_big / (t_big * 1e-3)},
+            "note": "zncc FLOPs per centre = offsets x 6 x window pixels; the FP32 peak is nominal "
+                    "(no measured CUDA-core peak); both kernels run once per sequence (its first frame)"}
+
+
 # ---------------------------------------------------------------------------
 # implicit adjoint: noise propagation and finite differences
 # ---------------------------------------------------------------------------
@@ -997,6 +1052,7 @@ def run_ours(args, ws, rank, local):
                                                   label="small_frame_stream")
     if not args.no_local:
         out["local_refinement"] = run_local(args, dev, wl, dic)
+        out["init_motion"] = run_init_motion(args, dev, wl)
     if not args.no_batch:
         out["batched"] = run_batched(args, dev)
     if not args.no_adjoint:

@@ -109,6 +109,8 @@ _SIGS = {
     "d2ic_zncc_match":(i32, [vp, i32, i32, vp, i32, i32, vp, i32, i32, i32, vp, vp, vp]),
     "d2ic_idw_project": (i32, [vp, i32, vp, vp, i32, f32, vp, vp]),
     "d2ic_strain_gl": (i32, [vp, vp, vp, vp, i32, i32, f32, f32, vp, vp, vp]),
+    "d2ic_strain_gl_jvp_work_doubles": (szt, [i32, i32]),
+    "d2ic_strain_gl_jvp": (i32, [vp, vp, i32, vp, vp, vp, i32, i32, f64, f64, vp, vp, vp]),
     "d2ic_discrepancy_map": (i32, [vp, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),
     "d2ic_central_gradient": (i32, [vp, i32, i32, vp, vp, vp]),
     "d2ic_local_coordinates": (i32, [vp, vp, vp, ctypes.c_longlong, i32, vp, vp, vp]),

@@ -203,37 +203,23 @@ def newton_polish(solver, state, def_image, u, alpha_reg: float, steps: int = 3,
 def strain_jvp(u, du, nodes, nbr_index, nbr_degree, gauge_length: float = 0.0, eps: float = 1e-8):
     """Linearised Green-Lagrange Voigt strain: d voigt for displacement directions du (K, Nn, 2).
 
-    Same weighted least squares as d2ic/strain.py:11-92 (FP64 torch), differentiated:
-    G = A^-1 B(u), dE = (dG^T F + F^T dG) / 2 with F = I + G.
+    Same weighted least squares as d2ic/strain.py:11-92, differentiated (FP64, on the device:
+    d2ic_strain_gl_jvp): G = A^-1 B(u), dE = (dG^T F + F^T dG) / 2 with F = I + G.
     """
     dev = du.device
-    u = torch.as_tensor(u, dtype=torch.float64, device=dev).reshape(-1, 2)
-    X = torch.as_tensor(np.asarray(nodes), dtype=torch.float64, device=dev).reshape(-1, 2)
-    idx = torch.as_tensor(np.asarray(nbr_index), dtype=torch.long, device=dev)
-    deg = torch.as_tensor(np.asarray(nbr_degree), dtype=torch.long, device=dev)
-    n, md = idx.shape
-    mask = torch.arange(md, device=dev)[None, :] < deg[:, None]
-    nid = torch.where(mask, idx, torch.zeros_like(idx))
-    dX = X[nid] - X[:, None, :]
-    w = mask.to(torch.float64)
-    if gauge_length > 0:
-        r = torch.linalg.norm(dX, dim=2)
-        w = w * torch.exp(-(r / (gauge_length + 1e-12)) ** 2)
-    A = torch.einsum("nk,nki,nkj->nij", w, dX, dX) + eps * torch.eye(2, dtype=torch.float64, device=dev)
-    det = A[:, 0, 0] * A[:, 1, 1] - A[:, 0, 1] * A[:, 1, 0]          # closed-form 2x2 inverse
-    Ainv = torch.stack([torch.stack([A[:, 1, 1], -A[:, 0, 1]], -1),
-                        torch.stack([-A[:, 1, 0], A[:, 0, 0]], -1)], -2) / det[:, None, None]
-
-    def grad_of(v):                         # v (..., Nn, 2) -> G (..., Nn, 2, 2), G[c][i] = d v_c / d x_i
-        dv = v[..., nid, :] - v[..., :, None, :]
-        Bm = torch.einsum("nk,nki,...nkc->...nic", w, dX, dv)
-        return torch.einsum("nij,...njc->...nci", Ainv, Bm)
-
-    G = grad_of(u)
-    F = torch.eye(2, dtype=torch.float64, device=dev) + G
-    dG = grad_of(du.to(torch.float64))
-    dE = 0.5 * (dG.transpose(-1, -2) @ F + F.transpose(-1, -2) @ dG)
-    return torch.stack([dE[..., 0, 0], dE[..., 1, 1], 0.5 * (dE[..., 0, 1] + dE[..., 1, 0])], dim=-1)
+    u = torch.as_tensor(u, dtype=torch.float64, device=dev).reshape(-1, 2).contiguous()
+    X = torch.as_tensor(np.asarray(nodes, dtype=np.float64), device=dev).reshape(-1, 2).contiguous()
+    idx = torch.as_tensor(np.ascontiguousarray(np.asarray(nbr_index), dtype=np.int32), device=dev)
+    deg = torch.as_tensor(np.ascontiguousarray(np.asarray(nbr_degree), dtype=np.int32), device=dev)
+    n = X.shape[0]
+    md = int(idx.shape[1]) if idx.ndim == 2 else 0
+    dd = du.to(torch.float64).reshape(-1, n, 2).contiguous()
+    K = dd.shape[0]
+    work = torch.empty(int(_lib.load().d2ic_strain_gl_jvp_work_doubles(n, md)) or 1, dtype=torch.float64, device=dev)
+    out = torch.empty((K, n, 3), dtype=torch.float64, device=dev)
+    _lib.call("d2ic_strain_gl_jvp", ptr(u), ptr(dd), K, ptr(X), ptr(idx), ptr(deg), n, md, float(gauge_length),
+              float(eps), ptr(work), ptr(out), _lib.stream_handle())
+    return out.reshape(tuple(du.shape[:-2]) + (n, 3))
 
 
 class _DICSolveFn(torch.autograd.Function):

@@ -3,7 +3,7 @@
 //
 // ZNCC (d2ic/solver_translation_zncc.py:89-168): one block per centre; the
 // template (win x win) and the search patch ((win + 2 s)^2) are staged in
-// shared memory; each thread scores a subset of the (2 s + 1)^2 offsets with a
+// shared memory; each thread scores one (up to 1024 offsets) or several of the (2 s + 1)^2 offsets with a
 // two-pass (mean, then centred sums) window normalisation; the block keeps the
 // first maximum in row-major (ky, kx) order.  FP32 arithmetic on the CUDA
 // cores: nothing here is a dense contraction.
@@ -11,7 +11,7 @@
 
 namespace d2ic {
 
-__global__ void zncc_kernel(const float *__restrict__ ref, int Hr, int Wr, const float *__restrict__ def, int Hd,
+__global__ void __launch_bounds__(1024) zncc_kernel(const float *__restrict__ ref, int Hr, int Wr, const float *__restrict__ def, int Hd,
                             int Wd, const float2 *__restrict__ centers, int win, int search, float2 *__restrict__ u_out,
                             float *__restrict__ score_out) {
     extern __shared__ float sm[];
@@ -128,55 +128,83 @@ __global__ void zncc_kernel(const float *__restrict__ ref, int Hr, int Wr, const
     }
 }
 
-// IDW (power p) of centre displacements onto nodes.  FP64 sqrt/divide are
-// slow on GB300, so per-pair math is FP32 (squared distances of pixel-grid
-// coordinates are exact in FP32 up to 2^24) with Kahan-compensated FP32 sums
-// inside each 256-centre tile and FP64 accumulation across tiles.
-__global__ void idw_kernel(const float2 *__restrict__ nodes, int n_nodes, const float2 *__restrict__ centers,
-                           const float2 *__restrict__ disp, int nc, float power, float2 *__restrict__ out) {
-    __shared__ float2 sc[256], sd[256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const float2 p = (i < n_nodes) ? nodes[i] : make_float2(0.f, 0.f);
-    double sw = 0.0, sx = 0.0, sy = 0.0;
-    int exact = -1;
-    float2 ev = make_float2(0.f, 0.f);
+// IDW (power p) of centre displacements onto nodes: one warp per NPW nodes (8 warps per block; 4
+// nodes on large meshes, 1 where 4 would leave SMs idle), the centres staged in shared-memory tiles
+// of 256 that the block's warps share; lane l takes centres l, l + 32, ... of each tile against all
+// of the warp's nodes, so one centre read serves NPW pairs.  FP64 sqrt/divide are slow on GB300, so per-pair math is FP32 (squared
+// distances of pixel-grid coordinates are exact in FP32 up to 2^24) with the reciprocal correctly
+// rounded; each lane sums a tile (8 centres) in FP32 and adds that into FP64 accumulators, and the
+// lanes' FP64 sums are reduced over the warp at the end.  A centre closer than 1e-6 gives the node
+// its displacement: the smallest such centre index, tracked without a branch (its infinite weight
+// is discarded).  Centres with a NaN displacement are dropped.
+constexpr int IDW_TILE = 256;
+template <int IDW_NODES>
+__global__ void __launch_bounds__(256) idw_kernel(const float2 *__restrict__ nodes, int n_nodes,
+                                                  const float2 *__restrict__ centers, const float2 *__restrict__ disp,
+                                                  int nc, float power, float2 *__restrict__ out) {
+    __shared__ float2 sc[IDW_TILE], sd[IDW_TILE];
+    const int lane = threadIdx.x & 31;
+    const int i0 = (blockIdx.x * 8 + (threadIdx.x >> 5)) * IDW_NODES;
+    float2 p[IDW_NODES];
+    double sw[IDW_NODES], sx[IDW_NODES], sy[IDW_NODES];
+    int ex[IDW_NODES];
+#pragma unroll
+    for (int j = 0; j < IDW_NODES; ++j) {
+        p[j] = (i0 + j < n_nodes) ? nodes[i0 + j] : make_float2(0.f, 0.f);
+        sw[j] = sx[j] = sy[j] = 0.0;
+        ex[j] = 0x7fffffff;
+    }
     const bool p2 = (power == 2.0f);
-    for (int base = 0; base < nc; base += 256) {
-        const int m = min(256, nc - base);
+    for (int base = 0; base < nc; base += IDW_TILE) {
+        const int m = min(IDW_TILE, nc - base);
         __syncthreads();
-        if (threadIdx.x < m) {
+        if ((int)threadIdx.x < m) {
             sc[threadIdx.x] = centers[base + threadIdx.x];
             sd[threadIdx.x] = disp[base + threadIdx.x];
         }
         __syncthreads();
-        if (i < n_nodes && exact < 0) {
-            float tw = 0.f, tx = 0.f, ty = 0.f, cw = 0.f, cx = 0.f, cy = 0.f;   // tile sums + compensation
-            for (int k = 0; k < m; ++k) {
-                const float2 d = sd[k];
-                if (d.x != d.x || d.y != d.y) continue;      // centres with NaN displacement are dropped
-                const float dx = sc[k].x - p.x, dy = sc[k].y - p.y;
+        if (i0 >= n_nodes) continue;
+        float tw[IDW_NODES], tx[IDW_NODES], ty[IDW_NODES];
+#pragma unroll
+        for (int j = 0; j < IDW_NODES; ++j) tw[j] = tx[j] = ty[j] = 0.f;
+        for (int k = lane; k < m; k += 32) {
+            const float2 d = sd[k];
+            if (d.x != d.x || d.y != d.y) continue;      // centres with NaN displacement are dropped
+            const float2 c = sc[k];
+#pragma unroll
+            for (int j = 0; j < IDW_NODES; ++j) {
+                const float dx = c.x - p[j].x, dy = c.y - p[j].y;
                 const float d2 = dx * dx + dy * dy;
-                if (d2 < 1e-12f) {                            // dist < 1e-6: take this centre's value
-                    exact = base + k;
-                    ev = d;
-                    break;
-                }
-                const float w = p2 ? 1.0f / d2 : powf(sqrtf(d2), -power);
-                float y = w - cw, t = tw + y;
-                cw = (t - tw) - y;
-                tw = t;
-                y = w * d.x - cx; t = tx + y; cx = (t - tx) - y; tx = t;
-                y = w * d.y - cy; t = ty + y; cy = (t - ty) - y; ty = t;
+                ex[j] = d2 < 1e-12f ? min(ex[j], base + k) : ex[j];   // dist < 1e-6
+                const float w = p2 ? __frcp_rn(d2) : powf(sqrtf(d2), -power);
+                tw[j] += w;
+                tx[j] += w * d.x;
+                ty[j] += w * d.y;
             }
-            sw += (double)tw - (double)cw;
-            sx += (double)tx - (double)cx;
-            sy += (double)ty - (double)cy;
+        }
+#pragma unroll
+        for (int j = 0; j < IDW_NODES; ++j) {
+            sw[j] += (double)tw[j];
+            sx[j] += (double)tx[j];
+            sy[j] += (double)ty[j];
         }
     }
-    if (i >= n_nodes) return;
-    if (exact >= 0) out[i] = ev;
-    else if (sw > 0.0) out[i] = make_float2((float)(sx / sw), (float)(sy / sw));
-    else out[i] = make_float2(0.f, 0.f);
+    if (i0 >= n_nodes) return;
+#pragma unroll
+    for (int j = 0; j < IDW_NODES; ++j) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sw[j] += __shfl_xor_sync(0xffffffffu, sw[j], o);
+            sx[j] += __shfl_xor_sync(0xffffffffu, sx[j], o);
+            sy[j] += __shfl_xor_sync(0xffffffffu, sy[j], o);
+            ex[j] = min(ex[j], __shfl_xor_sync(0xffffffffu, ex[j], o));
+        }
+        if (lane == j && i0 + j < n_nodes) {
+            if (ex[j] != 0x7fffffff) out[i0 + j] = disp[ex[j]];
+            else if (sw[j] > 0.0) out[i0 + j] = make_float2((float)(sx[j] / sw[j]), (float)(sy[j] / sw[j]));
+            else out[i0 + j] = make_float2(0.f, 0.f);
+        }
+    }
 }
 
 }  // namespace d2ic
@@ -196,8 +224,12 @@ extern "C" int d2ic_zncc_match(const float *ref, int Hr, int Wr, const float *de
         cudaError_t e = cudaFuncSetAttribute(zncc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return cuda_status(e, "zncc smem attribute");
     }
-    zncc_kernel<<<n_centers, 256, smem, (cudaStream_t)stream>>>(ref, Hr, Wr, def, Hd, Wd, (const float2 *)centers, win,
-                                                               search, (float2 *)u_out, score_out);
+    // one thread per offset where they fit in a block (289 offsets at search 8: 320 threads), so that
+    // no thread scores a second offset while the others wait
+    const int npa = 2 * search + 1;
+    const int threads = npa * npa >= 1024 ? 1024 : ((npa * npa + 31) / 32) * 32;
+    zncc_kernel<<<n_centers, threads < 64 ? 64 : threads, smem, (cudaStream_t)stream>>>(
+        ref, Hr, Wr, def, Hd, Wd, (const float2 *)centers, win, search, (float2 *)u_out, score_out);
     D2IC_CHECK_LAUNCH("zncc_kernel");
     return D2IC_OK;
 }
@@ -207,8 +239,13 @@ extern "C" int d2ic_idw_project(const float *nodes, int n_nodes, const float *ce
     D2IC_REQUIRE(nodes && u_out && (n_centers == 0 || (centers && disp)), "d2ic_idw_project: null pointer");
     D2IC_REQUIRE(n_nodes >= 0 && n_centers >= 0, "d2ic_idw_project: bad sizes");
     if (n_nodes == 0) return D2IC_OK;
-    idw_kernel<<<(n_nodes + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
-        (const float2 *)nodes, n_nodes, (const float2 *)centers, (const float2 *)disp, n_centers, power, (float2 *)u_out);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_nodes >= 4 * 8 * 912)   // at least ~2 waves of 4-node warps (3 blocks per SM on 152 SMs)
+        idw_kernel<4><<<(n_nodes + 31) / 32, 256, 0, s>>>((const float2 *)nodes, n_nodes, (const float2 *)centers,
+                                                          (const float2 *)disp, n_centers, power, (float2 *)u_out);
+    else
+        idw_kernel<1><<<(n_nodes + 7) / 8, 256, 0, s>>>((const float2 *)nodes, n_nodes, (const float2 *)centers,
+                                                        (const float2 *)disp, n_centers, power, (float2 *)u_out);
     D2IC_CHECK_LAUNCH("idw_kernel");
     return D2IC_OK;
 }

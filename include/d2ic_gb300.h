@@ -437,6 +437,18 @@ D2IC_API int d2ic_strain_gl(const float *u, const float *nodes, const int *nbr_i
                    int n_nodes, int max_deg, float gauge_length, float eps,
                    float *voigt_out, float *F_out, void *stream);
 
+/* Linearised strain for K displacement directions (the strain sensitivity of the implicit adjoint;
+ * the derivative of d2ic/strain.py:11-92 with respect to u): u (n_nodes, 2) FP64 is the
+ * linearisation point, du (K, n_nodes, 2) FP64 the directions, nodes (n_nodes, 2) FP64;
+ * dvoigt_out (K, n_nodes, 3) FP64 = [dE00, dE11, (dE01 + dE10) / 2] with dE = (dG^T F + F^T dG) / 2,
+ * F = I + G(u), dG = G(du), G the same weighted least-squares gradient as d2ic_strain_gl.
+ * work: d2ic_strain_gl_jvp_work_doubles(n_nodes, max_deg) doubles of device scratch.
+ * No counterpart in the reference (its strain is differentiated by JAX autodiff). */
+D2IC_API size_t d2ic_strain_gl_jvp_work_doubles(int n_nodes, int max_deg);
+D2IC_API int d2ic_strain_gl_jvp(const double *u, const double *du, int K, const double *nodes, const int *nbr_index,
+                       const int *nbr_degree, int n_nodes, int max_deg, double gauge_length, double eps,
+                       double *work, double *dvoigt_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -169,6 +169,29 @@ def test_idw_matches_oracle(cuda):
     assert np.abs(out - ref).max() <= 1e-5
 
 
+@pytest.mark.parametrize("nx,ny", [(52, 35), (176, 168)])
+def test_idw_many_centres_matches_oracle(cuda, nx, ny):
+    """Several 256-centre tiles (lanes split each tile), two exact centres for one node (the first in
+    centre order wins), dropped NaN centres in several tiles, and node counts that are not multiples
+    of a block's nodes; 176 x 168 nodes take the four-nodes-per-warp kernel."""
+    from d2ic_gb300.dic_init_motion import project_centers_to_nodes_idw_device
+    from oracle.init_motion import project_centers_to_nodes_idw
+    rng = np.random.default_rng(5)
+    nodes = np.stack(np.meshgrid(np.arange(nx) * 12.0, np.arange(ny) * 12.0), -1).reshape(-1, 2)[:-3]
+    hi = 12 * max(nx, ny)
+    centers = rng.integers(0, hi * 8, (1100, 2)) / 8.0      # exact in float32, as pixel-grid centres are
+    disp = rng.normal(0, 2, (1100, 2))
+    centers[700] = nodes[40]
+    centers[900] = nodes[40]
+    centers[300] = nodes[41]
+    disp[[10, 333, 1000]] = np.nan
+    out = project_centers_to_nodes_idw_device(nodes, centers, disp).cpu().numpy()
+    ref = project_centers_to_nodes_idw(nodes, centers, disp)
+    assert np.array_equal(out[40], disp[700].astype(np.float32))
+    assert np.array_equal(out[41], disp[300].astype(np.float32))
+    assert np.abs(out - ref).max() <= 1e-5
+
+
 def test_strain_matches_oracle(cuda):
     import d2ic_gb300 as d2
     from oracle.mesh import node_neighbor_tables
