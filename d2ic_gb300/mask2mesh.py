@@ -40,8 +40,12 @@ def _remove_small_components(mask: np.ndarray, min_area: int) -> np.ndarray:
     if not mask.any():
         return mask
     labels, n = ndimage.label(mask, structure=[[0, 1, 0], [1, 1, 1], [0, 1, 0]])
+    if n == 1:                                       # one component: its area is the mask's
+        return mask if int(np.count_nonzero(mask)) >= max(1, min_area) else np.zeros_like(mask)
     area = np.bincount(labels.ravel(), minlength=n + 1)
     keep = area >= max(1, min_area)
+    if keep[1:].all():
+        return mask                                  # every component is kept: the mask as it is
     keep[0] = False
     return keep[labels]
 
@@ -90,10 +94,10 @@ def mask_to_mesh_assets(mask: np.ndarray, element_size_px: float, binning: int =
                         origin_xy: Tuple[float, float] = (0.0, 0.0), enforce_quads: bool = True,
                         remove_islands: bool = True, min_island_area_px: int = 64):
     """``(mesh, MeshAssets(mesh, centres, roi_mask=binned mask))`` (d2ic/mask2mesh.py:145-182)."""
-    mesh = mask_to_mesh(mask, element_size_px, binning, origin_xy, enforce_quads, remove_islands, min_island_area_px)
     m = np.asarray(mask, dtype=bool)
-    if remove_islands:
+    if remove_islands:                               # islands removed once, for the mesh and the ROI
         m = _remove_small_components(m, min_island_area_px)
+    mesh = mask_to_mesh(m, element_size_px, binning, origin_xy, enforce_quads, False, min_island_area_px)
     roi = downsample_mask(m, binning)
     return mesh, MeshAssets(mesh=mesh, element_centers_xy=compute_element_centers(mesh), pixel_data=None,
                             roi_mask=roi)
