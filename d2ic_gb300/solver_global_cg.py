@@ -167,7 +167,7 @@ class GlobalCGSolver(SolverBase):
         if wait:
             torch.cuda.current_stream(self._device).synchronize()
         n_iters, status = int(pi[0]), int(pi[1])
-        if status in (_lib.WAIT_TIMEOUT, _lib.CUDA_ERROR):
+        if status in (_lib.WAIT_TIMEOUT, _lib.CUDA_ERROR, _lib.INTERNAL):
             raise _lib.D2ICError(status, "CG engine aborted")
         if self._verbose and self._log_cg:
             for k in range(min(n_iters + 1, ph.shape[0])):
