@@ -548,9 +548,11 @@ def run_serving_stream(args, dev):
     diffs = {key: float(np.abs(done[key].u - u).max()) for key, u in plain_u.items()}
     diff = max(diffs.values())
     side_of = {q.seq_id: q.side for q in seqs}
-    svc_by_side = {}
+    svc_by_side, svc_by_elem = {}, {}
+    elem_of = {q.seq_id: q.element_px for q in seqs}
     for (s_id, _k), t in zip(st.order[:n_plain], svc):
         svc_by_side.setdefault(side_of[s_id], []).append(t)
+        svc_by_elem.setdefault((side_of[s_id], elem_of[s_id]), []).append(t)
     it_capped = sum(1 for r in reqs if r.n_iters is not None and r.n_iters >= seqs[r.seq_id].config.max_iters)
     sweep = []
     for rate in args.stream_rates:
@@ -583,6 +585,8 @@ def run_serving_stream(args, dev):
             "plain_service_ms_p50_by_side": {str(k): 1000 * float(np.percentile(v, 50))
                                              for k, v in sorted(svc_by_side.items())},
             "plain_seconds_by_side": {str(k): float(np.sum(v)) for k, v in sorted(svc_by_side.items())},
+            "plain_service_ms_p50_by_side_and_element": {f"{a}px_e{b}": 1000 * float(np.percentile(v, 50))
+                                                         for (a, b), v in sorted(svc_by_elem.items())},
             "frames_at_max_iters": it_capped,
             "rate_sweep": sweep, "parity_sampled": parity, "slots": min(len(seqs), args.stream_slots),
             "slice_rounds": args.serve_slice, "graphs": sorted(srv.graphs), "long_slices": srv.long_slices,
