@@ -299,17 +299,27 @@ class FrameLayout:
 
     @staticmethod
     def _tile_shape(kind: int, chunk_box: np.ndarray, W: int, H: int):
-        """Shared-memory coefficient tile per chunk (cubic): the chunk's largest pixel box plus the
-        4x4 stencil (3), a 2-pixel margin each side (4), one pixel of spread between the element's
-        nodes (1) and, in x, up to 3 columns lost to the 16-byte TMA alignment."""
+        """Shared-memory coefficient tile per chunk (cubic): a chunk's pixel box plus the 4x4
+        stencil (3), a 2-pixel margin each side (4), one pixel of spread between the element's
+        nodes (1) and, in x, up to 3 columns lost to the 16-byte TMA alignment.  Sized for the
+        largest box when that fits in TILE_MAX_FLOATS, else for the 90th percentile of the boxes'
+        widths and heights (a few partly covered elements, e.g. on an ellipse boundary, can make one
+        chunk's box much larger than the rest): a chunk whose box exceeds the tile reads the pixels
+        outside it from global memory with the same arithmetic, so the tile changes no result."""
         if kind != _lib.INTERP_CUBIC or chunk_box.shape[0] == 0 or W + 2 * PAD >= 32768 or H + 2 * PAD >= 32768:
             return 0, 0
         b0 = chunk_box[:, 0].astype(np.int64) & 0xFFFFFFFF
         b1 = chunk_box[:, 1].astype(np.int64) & 0xFFFFFFFF
-        cw = int(((b1 & 0xFFFF) - (b0 & 0xFFFF)).max()) + 1
-        ch = int(((b1 >> 16) - (b0 >> 16)).max()) + 1
-        tw = (cw + 11 + 3) // 4 * 4
-        th = ch + 8
+        cws = (b1 & 0xFFFF) - (b0 & 0xFFFF) + 1
+        chs = (b1 >> 16) - (b0 >> 16) + 1
+
+        def shape(cw, ch):
+            return (int(cw) + 11 + 3) // 4 * 4, int(ch) + 8
+
+        tw, th = shape(cws.max(), chs.max())
+        if tw * th <= _lib.TILE_MAX_FLOATS:
+            return tw, th
+        tw, th = shape(np.percentile(cws, 90, method="higher"), np.percentile(chs, 90, method="higher"))
         return (tw, th) if tw * th <= _lib.TILE_MAX_FLOATS else (0, 0)
 
     @classmethod
