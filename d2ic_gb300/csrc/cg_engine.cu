@@ -683,7 +683,7 @@ __device__ __forceinline__ void node_post(const d2ic_frame_t &F, const FInfo &fi
     DF sj = {0.f, 0.f};
     const int K = F.node_chunk_k, Nn = F.n_nodes;
     const float4 *ng = reinterpret_cast<const float4 *>(F.node_grad) + n;
-    constexpr int NB = 4;
+    constexpr int NB = 8;
     for (int kb = 0; kb < K; kb += NB) {
         float4 v[NB];
 #pragma unroll
