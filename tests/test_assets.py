@@ -95,3 +95,50 @@ def test_host_helpers_match_numpy_forms():
             pc = pc[mask[rows, cols]]
         r, c = _roi_pixels(nodes, H, W, 2.0, mask)
         assert np.array_equal(np.stack([c + 0.5, r + 0.5], axis=1), pc)
+
+
+def test_island_removal_fast_paths_equal_the_general_rule():
+    """One component (kept or dropped) and several components all kept take shortcuts in
+    _remove_small_components; each must equal the flood-fill rule of the oracle."""
+    from d2ic_gb300.mask2mesh import _remove_small_components
+    one = np.zeros((40, 50), bool)
+    one[5:30, 8:40] = True
+    two = one.copy()
+    two[33:38, 44:49] = True                      # a second component of 25 pixels
+    tiny = np.zeros((40, 50), bool)
+    tiny[3:5, 3:5] = True                         # one component of 4 pixels
+    for m, a in ((one, 64), (one, 2000), (two, 10), (two, 64), (tiny, 3), (tiny, 5)):
+        got = _remove_small_components(m, a)
+        assert np.array_equal(got, om.remove_small_components_floodfill(m, a)), (int(m.sum()), a)
+
+
+def test_mask_to_mesh_assets_removes_islands_once():
+    """The mesh and the ROI of mask_to_mesh_assets come from the same cleaned mask."""
+    m = ellipse_mask(300, 260, np.random.default_rng(3))
+    m[5:9, 5:9] = True                            # an island below the default 64 pixels
+    mesh, assets = d2.mask_to_mesh_assets(m, 12)
+    ref_mesh = d2.mask_to_mesh(m, 12)
+    assert np.array_equal(mesh.nodes_xy, ref_mesh.nodes_xy) and np.array_equal(mesh.elements, ref_mesh.elements)
+    assert not assets.roi_mask[5:9, 5:9].any() and assets.roi_mask.sum() == (m.sum() - 16)
+
+
+def test_tile_shape_uses_the_90th_percentile_when_the_largest_box_does_not_fit():
+    """Coefficient tile per chunk: the largest pixel box when it fits in TILE_MAX_FLOATS, else the
+    90th percentile of the boxes' sides (chunks beyond it read the rest from global memory)."""
+    from d2ic_gb300 import _lib
+    from d2ic_gb300.engine import FrameLayout
+
+    def boxes(sizes):
+        b = []
+        for k, (w, h) in enumerate(sizes):
+            x0, y0 = 40 * k, 10
+            b.append([x0 | (y0 << 16), (x0 + w - 1) | ((y0 + h - 1) << 16)])
+        return np.asarray(b, np.int64).astype(np.uint32).view(np.int32)
+
+    regular = boxes([(16, 16)] * 20)
+    assert FrameLayout._tile_shape(_lib.INTERP_CUBIC, regular, 512, 512) == (28, 24)
+    outliers = boxes([(32, 8)] * 30 + [(32, 18), (30, 24)])          # the largest needs 44 x 32 > 736
+    assert FrameLayout._tile_shape(_lib.INTERP_CUBIC, outliers, 1024, 1024) == (44, 16)
+    huge = boxes([(60, 60)] * 10)
+    assert FrameLayout._tile_shape(_lib.INTERP_CUBIC, huge, 1024, 1024) == (0, 0)
+    assert FrameLayout._tile_shape(_lib.INTERP_LINEAR, regular, 512, 512) == (0, 0)
