@@ -67,6 +67,9 @@ def parse():
     p.add_argument("--stream-frames", type=int, default=4096)
     p.add_argument("--stream-seqs", type=int, default=128)
     p.add_argument("--stream-plain-frames", type=int, default=4096)
+    p.add_argument("--stream-hold-pixels", type=int, default=5_000_000,
+                   help="serving stream: size priority threshold in ROI pixels (ServeConfig.hold_pixels; "
+                        "the 4096^2 frames sit out slices while smaller frames are in flight; 0: off)")
     p.add_argument("--stream-slots", type=int, default=64,
                    help="frames in flight in the server (the engine keeps up to 64 active frames' lookup "
                         "tables in shared memory)")
@@ -522,7 +525,8 @@ def run_serving_stream(args, dev):
     plain_fps = n_plain / t_plain
 
     t0 = time.perf_counter()
-    srv = DICServer(dev, ServeConfig(max_slots=min(len(seqs), args.stream_slots), slice_rounds=args.serve_slice))
+    srv = DICServer(dev, ServeConfig(max_slots=min(len(seqs), args.stream_slots), slice_rounds=args.serve_slice,
+                                     hold_pixels=args.stream_hold_pixels))
     for q in seqs:
         srv.add_sequence(q.seq_id, q.ref, q.mesh, q.assets, q.config, init=q.init)
     t_srv_setup = time.perf_counter() - t0
@@ -589,6 +593,7 @@ def run_serving_stream(args, dev):
                                                          for (a, b), v in sorted(svc_by_elem.items())},
             "frames_at_max_iters": it_capped,
             "rate_sweep": sweep, "parity_sampled": parity, "slots": min(len(seqs), args.stream_slots),
+            "hold_pixels": args.stream_hold_pixels,
             "slice_rounds": args.serve_slice, "graphs": sorted(srv.graphs), "long_slices": srv.long_slices,
             "setup_s": {"stream": round(t_build, 1), "plain": round(t_plain_setup, 1),
                         "server": round(t_srv_setup, 1)},

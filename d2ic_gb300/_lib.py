@@ -25,7 +25,7 @@ CUDA_ERROR = -6
 UNSUPPORTED = -7
 INTERNAL = -8
 RUNNING = 1
-CMD_INIT, CMD_RUN, CMD_IDLE = 0, 1, 2
+CMD_INIT, CMD_RUN, CMD_IDLE, CMD_HOLD = 0, 1, 2, 3
 STOP_ON_FINISH, STOP_ON_IRQ = 1, 2
 
 INTERP_CUBIC = 0

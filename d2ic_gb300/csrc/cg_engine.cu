@@ -75,7 +75,7 @@ struct FrameState {
 };
 
 // per-frame commands written by the host between launches (control block, after the header)
-enum { CMD_INIT = 0, CMD_RUN = 1, CMD_IDLE = 2 };
+enum { CMD_INIT = 0, CMD_RUN = 1, CMD_IDLE = 2, CMD_HOLD = 3 };
 
 struct CtlHeader {
     unsigned bar_count;
@@ -109,7 +109,7 @@ enum { STOP_ON_FINISH = D2IC_STOP_ON_FINISH,   // after a round in which a frame
 // (blocks_past), so no block still reads an older round's copy either.
 struct Ctl {
     CtlHeader *h;
-    int *cmd;      // n_frames: CMD_INIT / CMD_RUN / CMD_IDLE
+    int *cmd;      // n_frames: CMD_INIT / CMD_RUN / CMD_IDLE / CMD_HOLD
     int *active;   // two copies of n_frames
     int *cpre;     // two copies of n_frames + 1
     int *gpre;     // two copies of n_frames + 1
@@ -853,13 +853,19 @@ __device__ __forceinline__ void block_scan3(int &a, int &b, int &c, int &ta, int
     __syncthreads();
 }
 
+// A frame takes part in this launch's rounds: not finished and not held (CMD_HOLD keeps an admitted
+// frame's state but leaves it out of the launch).  The command words are constant once r_init ran.
+__device__ __forceinline__ bool in_launch(Ctl &C, int f) {
+    return ld_vol(&C.fs[f].state) != ST_DONE && ld_vol(C.cmd + f) != CMD_HOLD;
+}
+
 // rebuild the active list and prefix sums (whole block)
 __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
     const int per = (n_frames + NT - 1) / NT;
     const int f0 = threadIdx.x * per, f1 = min(f0 + per, n_frames);
     int cnt = 0, ch = 0, gr = 0;
     for (int f = f0; f < f1; ++f)
-        if (ld_vol(&C.fs[f].state) != ST_DONE) {
+        if (in_launch(C, f)) {
             ++cnt;
             ch += frames[f].n_chunks;
             gr += pad_groups(frames[f].n_groups);
@@ -876,7 +882,7 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
     }
     int slot = cnt, cp = ch, gp = gr;
     for (int f = f0; f < f1; ++f)
-        if (ld_vol(&C.fs[f].state) != ST_DONE) {
+        if (in_launch(C, f)) {
             C.act(lb)[slot] = f;
             C.cp(lb)[slot] = cp;
             C.gp(lb)[slot] = gp;
@@ -888,9 +894,9 @@ __device__ void rebuild_active(const d2ic_frame_t *frames, int n_frames, Ctl &C)
 }
 
 // Start of a launch: new frames (CMD_INIT) get a fresh CG state, idle slots are
-// parked as finished-and-reported, running frames keep their state; frames
-// that finished in an earlier launch are marked reported (their outputs were
-// written at the end of that launch).
+// parked as finished-and-reported, running and held frames keep their state (held
+// ones stay out of the active list); frames that finished in an earlier launch are
+// marked reported (their outputs were written at the end of that launch).
 __device__ void r_init(const d2ic_frame_t *frames, int n_frames, Ctl &C) {
     for (int f = threadIdx.x; f < n_frames; f += NT) {
         const int cmd = ld_vol(C.cmd + f);
@@ -945,7 +951,7 @@ __device__ void rebuild_active_warp(const d2ic_frame_t *frames, int n_frames, Ct
     const int f0 = min(lane * per, n_frames), f1 = min(f0 + per, n_frames);
     int cnt = 0, ch = 0, gr = 0;
     for (int f = f0; f < f1; ++f)
-        if (ld_vol(&C.fs[f].state) != ST_DONE) {
+        if (in_launch(C, f)) {
             ++cnt;
             ch += frames[f].n_chunks;
             gr += pad_groups(frames[f].n_groups);
@@ -967,7 +973,7 @@ __device__ void rebuild_active_warp(const d2ic_frame_t *frames, int n_frames, Ct
     const int nb = 1 - __shfl_sync(0xffffffffu, lane == 0 ? ld_vol(&C.h->list_buf) : 0, 0);
     int slot = ic - cnt, cp = ih - ch, gp = ig - gr;
     for (int f = f0; f < f1; ++f)
-        if (ld_vol(&C.fs[f].state) != ST_DONE) {
+        if (in_launch(C, f)) {
             C.act(nb)[slot] = f;
             C.cp(nb)[slot] = cp;
             C.gp(nb)[slot] = gp;

@@ -67,6 +67,12 @@ class ServeConfig:
     # light load: with at most this many frames in flight and none waiting, one long slice runs at a
     # time and ends when a frame finishes or a new request can be admitted (0 turns this off)
     light_load_frames: int = 4
+    # size priority: while a frame with fewer than hold_pixels ROI pixels is in flight, frames with
+    # at least that many sit out slices (D2IC_CMD_HOLD; their state is kept, so results do not
+    # change), for at most hold_max_slices slices in a row; the engine advances all admitted frames
+    # by one evaluation per round, so this lets small frames finish at their own pace (0: off)
+    hold_pixels: int = 0
+    hold_max_slices: int = 8
 
 
 @dataclass
@@ -121,6 +127,8 @@ class DICServer:
         self.engine = Engine(self.device, S)
         self.cmd = self.engine.commands(S)
         self.cmd.fill_(_lib.CMD_IDLE)
+        self.cmd_host = [_lib.CMD_IDLE] * S        # the host's copy of the command words
+        self.held = [0] * S                          # consecutive slices a slot's frame was held
         nb = _desc_bytes()
         self.desc_dev = torch.zeros(S * nb, dtype=torch.uint8, device=self.device)
         self.slots: list[tuple[FrameSlot, Request, _Sequence] | None] = [None] * S
@@ -300,6 +308,8 @@ class DICServer:
             hb.copy_(torch.frombuffer(bytearray(bytes(slot.desc)), dtype=torch.uint8))
             self.desc_dev[i * nb:(i + 1) * nb].copy_(hb, non_blocking=True)
             self.cmd[i] = _lib.CMD_INIT
+            self.cmd_host[i] = _lib.CMD_INIT
+            self.held[i] = 0
             self.status_dev[i, 1] = _lib.RUNNING
             self.slots[i] = (slot, req, seq, self.slices)    # first slice that sees the frame
             seq.in_flight = True
@@ -386,6 +396,7 @@ class DICServer:
             self.awaiting.append((req, seq, ev))
             self.slots[i] = None
             self.cmd[i] = _lib.CMD_IDLE
+            self.cmd_host[i] = _lib.CMD_IDLE
             seq.in_flight = False
             seq.frames_done += 1
             if seq.queue:
@@ -407,7 +418,27 @@ class DICServer:
                 keep.append((req, seq, ev))
         self.awaiting = keep
 
+    def _apply_holds(self):
+        """Command words of the next slice under the size priority (ServeConfig.hold_pixels).  Only
+        frames admitted in an earlier slice are touched: that slice consumed their CMD_INIT."""
+        hp = self.cfg.hold_pixels
+        if not hp:
+            return
+        occ = [(i, e) for i, e in enumerate(self.slots) if e is not None and e[3] < self.slices]
+        small = any(e[0].layout.n_pix < hp for _, e in self.slots_in_flight())
+        for i, e in occ:
+            hold = small and e[0].layout.n_pix >= hp and self.held[i] < self.cfg.hold_max_slices
+            want = _lib.CMD_HOLD if hold else _lib.CMD_RUN
+            if self.cmd_host[i] != want:
+                self.cmd[i] = want
+                self.cmd_host[i] = want
+            self.held[i] = self.held[i] + 1 if hold else 0
+
+    def slots_in_flight(self):
+        return [(i, e) for i, e in enumerate(self.slots) if e is not None]
+
     def _queue_slice(self, mode: str):
+        self._apply_holds()
         self._launch_slice(mode)                    # the kernel turns CMD_INIT into CMD_RUN as it admits
         p = self.parity
         self.status_host[p].copy_(self.status_dev, non_blocking=True)

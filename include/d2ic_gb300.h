@@ -302,13 +302,17 @@ D2IC_API int d2ic_cg_solve_batched(const d2ic_frame_t *frames, int n_frames, voi
  * between calls.  Before a call the host sets one command word per frame at
  * control + d2ic_cg_command_offset(): D2IC_CMD_INIT admits a new frame (u0,
  * image coefficients and outputs must be ready), D2IC_CMD_RUN continues (or
- * leaves finished frames alone), D2IC_CMD_IDLE parks an empty slot.  A frame
+ * leaves finished frames alone), D2IC_CMD_IDLE parks an empty slot, D2IC_CMD_HOLD
+ * keeps an admitted frame's state but leaves it out of this call (set it only
+ * after the call that consumed the frame's D2IC_CMD_INIT; the frame reports
+ * D2IC_RUNNING and continues where it stopped under D2IC_CMD_RUN).  A frame
  * that finishes during the call gets its outputs and final status written;
  * unfinished frames report D2IC_RUNNING.  Serves the batched/served form of
  * GlobalCGSolver.solve (d2ic/solver_global_cg.py:151-198) for many frames. */
 #define D2IC_CMD_INIT 0
 #define D2IC_CMD_RUN  1
 #define D2IC_CMD_IDLE 2
+#define D2IC_CMD_HOLD 3
 D2IC_API size_t d2ic_cg_command_offset(void);
 D2IC_API int d2ic_cg_slice(const d2ic_frame_t *frames, int n_frames, void *control, size_t control_bytes,
                            int interp_kind, int grid_blocks, int max_rounds, void *stream);

@@ -175,6 +175,26 @@ def test_light_load_slices_equal_short_slices(cuda):
         assert np.array_equal(q.strain, r.strain)
 
 
+@pytest.mark.parametrize("light", [0, 4])
+def test_held_frames_equal_short_slices(cuda, light):
+    """Size priority (ServeConfig.hold_pixels): the larger sequence's frames sit out slices while a
+    smaller frame is in flight (D2IC_CMD_HOLD) and resume where they stopped; every result must be
+    bitwise that of plain short slices, with fixed and with light-load (long) slices."""
+    import d2ic_gb300 as d2
+    from d2ic_gb300.serving import ServeConfig
+    seqs = _two_sequences()                        # ROI 160^2 = 25,600 px and 224^2 = 50,176 px
+    cfg = d2.MeshDICConfig(max_iters=60, tol=1e-4, reg_strength=0.1)
+    _, short = _served(cuda, seqs, cfg, ServeConfig(max_slots=4, slice_rounds=5, light_load_frames=0))
+    srv, held = _served(cuda, seqs, cfg, ServeConfig(max_slots=4, slice_rounds=5, light_load_frames=light,
+                                                     hold_pixels=40_000, hold_max_slices=3))
+    assert set(held) == set(short)
+    for key, r in short.items():
+        q = held[key]
+        assert q.n_iters == r.n_iters
+        assert np.array_equal(q.u, r.u)
+        assert np.array_equal(q.strain, r.strain)
+
+
 def test_slice_stops_when_a_frame_finishes(cuda, uneven):
     """d2ic_cg_slice_ex with D2IC_STOP_ON_FINISH ends after the first round in which a frame
     finishes: that frame's outputs are written, the others report RUNNING, and continuing in
