@@ -290,8 +290,7 @@ def rect_mask(H: int, W: int, h: int, w: int) -> np.ndarray:
 def plate_hole_mask(H: int = 2048, W: int = 2048, side: int = 1800, radius: float = 300.0) -> np.ndarray:
     """Centred square minus a centred disk (pixel centres tested)."""
     m = rect_mask(H, W, side, side)
-    ii, jj = np.mgrid[0:H, 0:W]
-    r2 = (jj + 0.5 - W / 2) ** 2 + (ii + 0.5 - H / 2) ** 2
+    r2 = (np.arange(W)[None, :] + 0.5 - W / 2) ** 2 + (np.arange(H)[:, None] + 0.5 - H / 2) ** 2
     return m & (r2 >= radius * radius)
 
 
@@ -304,5 +303,6 @@ def ellipse_mask(H: int, W: int, rng: np.random.Generator, cover_lo=0.4, cover_h
     b = aspect * a
     a = min(a, W / 2 - 4)
     b = min(b, H / 2 - 4)
-    ii, jj = np.mgrid[0:H, 0:W]
-    return ((jj + 0.5 - W / 2) / a) ** 2 + ((ii + 0.5 - H / 2) / b) ** 2 <= 1.0
+    tx = ((np.arange(W)[None, :] + 0.5 - W / 2) / a) ** 2          # the same terms per pixel, broadcast
+    ty = ((np.arange(H)[:, None] + 0.5 - H / 2) / b) ** 2
+    return tx + ty <= 1.0
